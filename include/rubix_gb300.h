@@ -1,0 +1,166 @@
+/*
+ * rubix_gb300 C ABI: the particle -> IFU datacube path of rubix as hand-written
+ * sm_103a CUDA kernels.
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer unless its comment says "host".
+ *   - All work is enqueued on `stream` (a cudaStream_t passed as void*); no call
+ *     synchronises the stream and no call allocates or frees device memory.
+ *     Functions that need scratch memory take a caller-provided `workspace`
+ *     whose size comes from the matching *_workspace_size() query.
+ *   - Return value: RUBIX_OK (0) or a negative RUBIX_E_* code; the message of the
+ *     last failing call on the calling host thread is returned by
+ *     rubix_last_error().  No function aborts or exits the process.
+ *   - float32 data, int32 indices, row-major layouts.  A datacube is
+ *     [n_spaxels][spaxel_stride] floats whose first n_wave entries of each row
+ *     are the spectrum of spaxel (iy, ix) = (s / nb, s % nb) -- rubix's
+ *     cube[y, x, lambda] after reshape (rubix/spectra/ifu.py:286-287).
+ *
+ * Each entry point names the rubix function(s) it replaces (path:line relative
+ * to the rubix project root).
+ */
+#ifndef RUBIX_GB300_H
+#define RUBIX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define RUBIX_API __attribute__((visibility("default")))
+#else
+#define RUBIX_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RUBIX_OK 0
+#define RUBIX_E_INVALID (-1)     /* null pointer, negative size, bad enum      */
+#define RUBIX_E_SHAPE (-2)       /* sizes inconsistent or beyond a kernel limit */
+#define RUBIX_E_WORKSPACE (-3)   /* workspace missing or too small              */
+#define RUBIX_E_CUDA (-4)        /* CUDA runtime or launch error                */
+#define RUBIX_E_DEVICE (-5)      /* a kernel raised its device error flag       */
+#define RUBIX_E_UNSUPPORTED (-6) /* valid request outside what is built        */
+
+#define RUBIX_ABI_VERSION 1
+
+/* Version of this ABI (RUBIX_ABI_VERSION). */
+RUBIX_API int rubix_abi_version(void);
+
+/* Message of the last failing call on this host thread ("" if none). */
+RUBIX_API const char* rubix_last_error(void);
+
+/* ------------------------------------------------------------------------- */
+/* (a) Spaxel assignment and stable sort by spaxel                           */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * mask_out[i] = 1 if min(edges) <= x_i <= max(edges) and likewise for y_i,
+ * else 0.  coords is [n][coord_stride] with x at column 0 and y at column 1.
+ * Replaces mask_particles_outside_aperture, rubix/telescope/utils.py:156-178
+ * (used by filter_particles, rubix/core/telescope.py:151-175).
+ */
+RUBIX_API int rubix_aperture_mask(const float* coords, int64_t n, int64_t coord_stride,
+                        const float* edges, int32_t n_edges, uint8_t* mask_out,
+                        void* stream);
+
+/*
+ * idx_out[i] = ix + nb*iy with ix = clip(digitize(x_i, edges) - 1, 0, nb-1),
+ * likewise iy, nb = n_edges - 1 (digitize with right=False; edges ascending).
+ * Bit-exact with square_spaxel_assignment, rubix/telescope/utils.py:78-152
+ * (step spaxel_assignment, rubix/core/telescope.py:81-126).
+ */
+RUBIX_API int rubix_spaxel_assign(const float* coords, int64_t n, int64_t coord_stride,
+                        const float* edges, int32_t n_edges, int32_t* idx_out,
+                        void* stream);
+
+RUBIX_API size_t rubix_spaxel_sort_workspace_size(int64_t n, int32_t n_segments);
+
+/*
+ * Stable sort of particles by spaxel index (LSD radix sort).  Particle i takes
+ * part if keep == NULL or keep[i] != 0, and 0 <= idx[i] < n_segments (ids
+ * outside are dropped, as jax.ops.segment_sum drops them in calculate_cube,
+ * rubix/spectra/ifu.py:286).  perm_out[j] is the original index of the j-th
+ * particle in (spaxel, original index) order; the first seg_offsets[n_segments]
+ * entries are the kept particles and seg_offsets[s] .. seg_offsets[s+1]-1 are
+ * those of spaxel s.  seg_offsets_out has n_segments + 1 entries.
+ * Replaces the grouping inside segment_sum (rubix/spectra/ifu.py:286).
+ */
+RUBIX_API int rubix_spaxel_sort(const int32_t* idx, const uint8_t* keep, int64_t n,
+                      int32_t n_segments, int32_t* perm_out, int32_t* seg_offsets_out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* (b) Fused SSP lookup + mass scaling + Doppler shift/resampling + cube     */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * Shared inputs of the accumulate kernels.
+ *   ssp_flux      [n_met][n_age][n_wave]   SSPGrid.flux (rubix/spectra/ssp/grid.py:28-31)
+ *   ssp_metallicity [n_met], ssp_age [n_age]  ascending grids (interp2d x, y)
+ *   ssp_wave_z    [n_wave] ascending, the float32 (1+z)*wavelength of
+ *                 cosmological_doppler_shift (rubix/spectra/ifu.py:66-80, core/ifu.py:261)
+ *   wave_t        [n_wave_t] ascending telescope grid (telescope.wave_seq)
+ *   mass, metallicity, age [n]; velocity [n][vel_stride], line-of-sight
+ *                 component `vel_component` (rubix_config.yml ifu.doppler)
+ *   perm, seg_offsets   output of rubix_spaxel_sort for n_segments spaxels
+ */
+RUBIX_API size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
+                                 int32_t n_wave);
+
+/*
+ * cube[s][0..n_wave_t) = sum over kept particles p of spaxel s of
+ *   resample(mass_p * interp2d_linear(Z_p, age_p), wave_z*exp(v_p/c), wave_t).
+ * Replaces calculate_spectra (rubix/core/ifu.py:29-123, ssp.method="linear"),
+ * scale_spectrum_by_mass (core/ifu.py:127-159), doppler_shift_and_resampling
+ * (core/ifu.py:226-295, spectra/ifu.py:168-266) and calculate_datacube
+ * (core/ifu.py:299-341, spectra/ifu.py:270-288), fused; no N x lambda array is
+ * materialised.  Deterministic: the same inputs give bit-identical cubes.
+ * n_wave_t <= 4096.
+ */
+RUBIX_API int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,
+                   const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                   int32_t n_age, int32_t n_wave, const float* wave_t, int32_t n_wave_t,
+                   const float* mass, const float* metallicity, const float* age,
+                   const float* velocity, int64_t vel_stride, int32_t vel_component,
+                   const int32_t* perm, const int32_t* seg_offsets, int32_t n_segments,
+                   int64_t n, float* cube, int64_t spaxel_stride, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* (c) PSF: per-wavelength 2-D convolution, separable Gaussian               */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * out[y][x][l] = sum_{i,j} ty[i] tx[j] in[y + oy - i][x + ox - j][l] with zero
+ * padding, oy = (m_y-1)/2, ox = (m_x-1)/2 ("same" mode of convolve2d).  ty/tx are
+ * HOST arrays of m_y/m_x taps (m_y, m_x <= 63).  With ty = tx = the normalised 1-D
+ * Gaussian this equals convolve2d(plane, gaussian_kernel_2d, mode="same") for every
+ * plane: apply_psf, rubix/telescope/psf/psf.py:33-58 with kernels.py:5-31 (step
+ * convolve_psf, rubix/core/psf.py:15-75).  in and out must not overlap.
+ */
+RUBIX_API int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx, int32_t n_wave_t,
+                  int64_t spaxel_stride_in, int64_t spaxel_stride_out, const float* ty,
+                  int32_t m_y, const float* tx, int32_t m_x, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* (d) LSF: 1-D convolution along wavelength                                 */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * out[r][t] = sum_j taps[j] * in[r][t + crop - j] (zero outside [0, n_wave_t)):
+ * the full convolution cropped to [crop, n_wave_t + crop).  taps is a HOST array
+ * of n_taps <= 255 values.  With the rubix Gaussian taps and crop = 12 this is
+ * apply_lsf, rubix/telescope/lsf/lsf.py:29-105 (step convolve_lsf,
+ * rubix/core/lsf.py:14-67).  in and out must not overlap.
+ */
+RUBIX_API int rubix_lsf_fwd(const float* in, float* out, int64_t n_rows, int32_t n_wave_t,
+                  int64_t row_stride_in, int64_t row_stride_out, const float* taps,
+                  int32_t n_taps, int32_t crop, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RUBIX_GB300_H */

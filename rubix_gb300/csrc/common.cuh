@@ -1,0 +1,66 @@
+// Shared helpers for the rubix_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <stdio.h>
+#include <stdarg.h>
+
+#include <algorithm>
+
+#include "../../include/rubix_gb300.h"
+
+namespace rubix {
+
+// Records a formatted message as this thread's last error and returns `code`.
+int set_error(int code, const char* fmt, ...);
+void clear_error();
+
+// Checks a CUDA runtime call; on failure records the error and returns RUBIX_E_CUDA.
+#define RUBIX_CUDA_TRY(expr)                                                        \
+  do {                                                                              \
+    cudaError_t _e = (expr);                                                        \
+    if (_e != cudaSuccess) {                                                        \
+      return ::rubix::set_error(RUBIX_E_CUDA, "%s failed: %s (%s:%d)", #expr,       \
+                                cudaGetErrorString(_e), __FILE__, __LINE__);        \
+    }                                                                               \
+  } while (0)
+
+#define RUBIX_LAUNCH_CHECK(name)                                                    \
+  do {                                                                              \
+    cudaError_t _e = cudaGetLastError();                                            \
+    if (_e != cudaSuccess) {                                                        \
+      return ::rubix::set_error(RUBIX_E_CUDA, "launch of %s failed: %s", name,      \
+                                cudaGetErrorString(_e));                            \
+    }                                                                               \
+  } while (0)
+
+#define RUBIX_REQUIRE(cond, code, ...)                                              \
+  do {                                                                              \
+    if (!(cond)) return ::rubix::set_error(code, __VA_ARGS__);                      \
+  } while (0)
+
+inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Bump allocator over a caller-provided workspace; sizes are rounded to 256 bytes.
+struct Carve {
+  char* base;
+  size_t off;
+  explicit Carve(void* p) : base(static_cast<char*>(p)), off(0) {}
+  template <class T>
+  T* take(size_t count) {
+    T* r = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += align_up(count * sizeof(T), 256);
+    return r;
+  }
+};
+
+int sm_count();  // cached multiprocessor count of the current device
+
+constexpr double kSpeedOfLight = 299792.458;  // km/s, rubix_config.yml:8
+constexpr float kFltMax = 3.402823466e+38f;
+
+}  // namespace rubix

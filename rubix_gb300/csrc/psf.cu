@@ -1,0 +1,135 @@
+// Kernel (c): separable 2-D convolution of every wavelength plane of a datacube
+// ("same" mode, zero padding).  A Gaussian PSF kernel normalised by its 2-D sum is
+// the outer product of two normalised 1-D Gaussians, so rubix's per-plane
+// convolve2d with gaussian_kernel_2d (telescope/psf/psf.py:33-58, kernels.py:5-31)
+// is an x-pass followed by a y-pass.
+//
+// A block owns a strip of kTileX spaxel columns by kTileL wavelengths (one warp
+// lane per wavelength: coalesced 128-byte row segments along the contiguous
+// wavelength axis) and streams down the y axis: each input row is staged in shared
+// memory with its x halo, convolved along x into a ring of the last m_y rows, and
+// the ring gives the y-convolved output row.  Every input element is read from
+// global memory once per strip (plus the x halo) and every output written once.
+#include "common.cuh"
+
+namespace rubix {
+namespace {
+
+constexpr int kPsfTileX = 32;
+constexpr int kPsfTileL = 32;
+constexpr int kPsfThreads = 256;
+constexpr int kPsfWarps = kPsfThreads / 32;
+constexpr int kPsfXPerThread = kPsfTileX / kPsfWarps;
+constexpr int kMaxTaps = 63;
+
+struct PsfArgs {
+  const float* in;
+  float* out;
+  int ny, nx, nl;
+  long long sin, sout;
+  int my, mx, oy, ox;
+  float ty[kMaxTaps + 1];
+  float tx[kMaxTaps + 1];
+};
+
+__global__ void __launch_bounds__(kPsfThreads) psf_strip_kernel(PsfArgs a) {
+  extern __shared__ float smem[];
+  const int wrow = kPsfTileX + a.mx - 1;
+  float* s_in = smem;                   // [wrow][kPsfTileL]
+  float* s_ring = smem + wrow * kPsfTileL;  // [my][kPsfTileX][kPsfTileL]
+  __shared__ float s_ty[kMaxTaps + 1], s_tx[kMaxTaps + 1];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < a.my) s_ty[tid] = a.ty[tid];
+  if (tid < a.mx) s_tx[tid] = a.tx[tid];
+  const int x0 = blockIdx.x * kPsfTileX;
+  const int l0 = blockIdx.y * kPsfTileL;
+  const int l = l0 + lane;
+  const int xsrc0 = x0 - (a.mx - 1) + a.ox;  // global x of s_in column 0
+  const int total = a.ny - 1 + a.oy;
+  for (int r = 0; r <= total; ++r) {
+    // 1. stage input row r (zero outside the cube)
+    for (int q = tid; q < wrow * kPsfTileL; q += kPsfThreads) {
+      const int jj = q / kPsfTileL, ll = q % kPsfTileL;
+      const int xg = xsrc0 + jj, lg = l0 + ll;
+      float v = 0.f;
+      if (r < a.ny && xg >= 0 && xg < a.nx && lg < a.nl)
+        v = a.in[((long long)r * a.nx + xg) * a.sin + lg];
+      s_in[q] = v;
+    }
+    __syncthreads();
+    // 2. x-pass into ring slot r % my
+    const int slot = r % a.my;
+#pragma unroll
+    for (int j = 0; j < kPsfXPerThread; ++j) {
+      const int xl = warp + kPsfWarps * j;
+      float h = 0.f;
+      for (int i = 0; i < a.mx; ++i)
+        h = fmaf(s_tx[i], s_in[(xl + (a.mx - 1) - i) * kPsfTileL + lane], h);
+      s_ring[(slot * kPsfTileX + xl) * kPsfTileL + lane] = h;
+    }
+    __syncthreads();
+    // 3. y-pass: output row y = r - oy
+    const int y = r - a.oy;
+    if (y >= 0 && y < a.ny && l < a.nl) {
+      const int imax = min(a.my - 1, r);
+#pragma unroll
+      for (int j = 0; j < kPsfXPerThread; ++j) {
+        const int xl = warp + kPsfWarps * j;
+        const int x = x0 + xl;
+        float o = 0.f;
+        int sl = slot;
+        for (int i = 0; i <= imax; ++i) {
+          o = fmaf(s_ty[i], s_ring[(sl * kPsfTileX + xl) * kPsfTileL + lane], o);
+          sl = (sl == 0) ? a.my - 1 : sl - 1;
+        }
+        if (x < a.nx) a.out[((long long)y * a.nx + x) * a.sout + l] = o;
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace rubix
+
+using namespace rubix;
+
+extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx,
+                             int32_t n_wave_t, int64_t spaxel_stride_in,
+                             int64_t spaxel_stride_out, const float* ty, int32_t m_y,
+                             const float* tx, int32_t m_x, void* stream) {
+  RUBIX_REQUIRE(ny >= 0 && nx >= 0 && n_wave_t >= 0, RUBIX_E_SHAPE, "rubix_psf_fwd: negative size");
+  RUBIX_REQUIRE(m_y >= 1 && m_y <= 31 && m_x >= 1 && m_x <= kMaxTaps, RUBIX_E_SHAPE,
+                "rubix_psf_fwd: kernel sizes must satisfy 1 <= m_y <= 31, 1 <= m_x <= %d",
+                kMaxTaps);
+  RUBIX_REQUIRE(spaxel_stride_in >= n_wave_t && spaxel_stride_out >= n_wave_t, RUBIX_E_SHAPE,
+                "rubix_psf_fwd: spaxel stride smaller than n_wave_t");
+  if (ny == 0 || nx == 0 || n_wave_t == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(in && out && ty && tx, RUBIX_E_INVALID, "rubix_psf_fwd: null pointer");
+  RUBIX_REQUIRE(in != out, RUBIX_E_INVALID, "rubix_psf_fwd: in and out must differ");
+  PsfArgs a;
+  a.in = in;
+  a.out = out;
+  a.ny = ny;
+  a.nx = nx;
+  a.nl = n_wave_t;
+  a.sin = spaxel_stride_in;
+  a.sout = spaxel_stride_out;
+  a.my = m_y;
+  a.mx = m_x;
+  a.oy = (m_y - 1) / 2;
+  a.ox = (m_x - 1) / 2;
+  for (int i = 0; i <= kMaxTaps; ++i) {
+    a.ty[i] = i < m_y ? ty[i] : 0.f;
+    a.tx[i] = i < m_x ? tx[i] : 0.f;
+  }
+  const size_t smem = sizeof(float) * ((size_t)(kPsfTileX + m_x - 1) * kPsfTileL +
+                                       (size_t)m_y * kPsfTileX * kPsfTileL);
+  cudaError_t e = cudaFuncSetAttribute(psf_strip_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess)
+    return set_error(RUBIX_E_CUDA, "cudaFuncSetAttribute(psf_strip_kernel): %s", cudaGetErrorString(e));
+  dim3 grid(div_up(nx, kPsfTileX), div_up(n_wave_t, kPsfTileL));
+  psf_strip_kernel<<<grid, kPsfThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+  RUBIX_LAUNCH_CHECK("psf_strip_kernel");
+  return RUBIX_OK;
+}

@@ -1,0 +1,302 @@
+// Kernel (a): aperture mask, spaxel assignment and a stable LSD radix sort of the
+// particles by spaxel index, ending in per-spaxel segment offsets.
+//
+// The radix sort is written from the published LSD scheme: per pass, a per-tile
+// digit histogram, one exclusive scan over (digit, tile), and a stable scatter in
+// which each tile ranks its keys with warp-level match/popc and per-warp digit
+// counters.  No float atomics anywhere; the result is deterministic.
+#include "common.cuh"
+#include "scan.cuh"
+
+namespace rubix {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kMaxSmemEdges = 8192;
+
+// Number of edges <= x (searchsorted side='right'); NaN counts as above all edges,
+// matching the NaN-last comparator of jnp.digitize.
+__device__ __forceinline__ int count_le(const float* e, int n, float x) {
+  if (x != x) return n;
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (e[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void aperture_mask_kernel(const float* __restrict__ coords, long long n,
+                                     long long stride, const float* __restrict__ edges,
+                                     int n_edges, unsigned char* __restrict__ mask) {
+  __shared__ float s_lo, s_hi;
+  if (threadIdx.x == 0) {
+    float lo = edges[0], hi = edges[0];
+    for (int i = 1; i < n_edges; ++i) {
+      lo = fminf(lo, edges[i]);
+      hi = fmaxf(hi, edges[i]);
+    }
+    s_lo = lo;
+    s_hi = hi;
+  }
+  __syncthreads();
+  const float lo = s_lo, hi = s_hi;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float x = coords[i * stride], y = coords[i * stride + 1];
+    mask[i] = (x >= lo && x <= hi && y >= lo && y <= hi) ? 1 : 0;
+  }
+}
+
+__global__ void spaxel_assign_kernel(const float* __restrict__ coords, long long n,
+                                     long long stride, const float* __restrict__ edges,
+                                     int n_edges, int* __restrict__ idx_out) {
+  extern __shared__ float s_edges[];
+  const bool in_smem = n_edges <= kMaxSmemEdges;
+  if (in_smem) {
+    for (int i = threadIdx.x; i < n_edges; i += blockDim.x) s_edges[i] = edges[i];
+    __syncthreads();
+  }
+  const float* e = in_smem ? s_edges : edges;
+  const int nb = n_edges - 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    int ix = count_le(e, n_edges, coords[i * stride]) - 1;
+    int iy = count_le(e, n_edges, coords[i * stride + 1]) - 1;
+    ix = min(max(ix, 0), nb - 1);
+    iy = min(max(iy, 0), nb - 1);
+    idx_out[i] = ix + nb * iy;
+  }
+}
+
+// key = idx if kept and inside [0, n_segments), else n_segments (sorts last).
+__global__ void make_keys_kernel(const int* __restrict__ idx,
+                                 const unsigned char* __restrict__ keep, long long n,
+                                 int n_segments, unsigned* __restrict__ keys,
+                                 int* __restrict__ vals) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    int k = idx[i];
+    bool ok = (k >= 0) && (k < n_segments) && (keep == nullptr || keep[i] != 0);
+    keys[i] = ok ? (unsigned)k : (unsigned)n_segments;
+    vals[i] = (int)i;
+  }
+}
+
+// Per-tile histogram of one digit; hist is digit-major: hist[d * n_tiles + tile].
+__global__ void __launch_bounds__(kSortThreads)
+radix_hist_kernel(const unsigned* __restrict__ keys, long long n, int shift,
+                  unsigned digit_mask, int n_tiles, int* __restrict__ hist) {
+  __shared__ int s_hist[kRadix];
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) s_hist[d] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kSortTile;
+  for (int it = 0; it < kSortItems; ++it) {
+    long long e = base + it * kSortThreads + threadIdx.x;
+    if (e < n) atomicAdd(&s_hist[(keys[e] >> shift) & digit_mask], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d <= (int)digit_mask; d += blockDim.x)
+    hist[(long long)d * n_tiles + blockIdx.x] = s_hist[d];
+}
+
+// Stable scatter of one digit pass.  Warp w of the tile owns the contiguous keys
+// [base + w*512, base + (w+1)*512) and walks them in 16 rounds of 32, so
+// (warp, round, lane) order equals input order.
+__global__ void __launch_bounds__(kSortThreads)
+radix_scatter_kernel(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
+                     unsigned* __restrict__ keys_out, int* __restrict__ vals_out, long long n,
+                     int shift, unsigned digit_mask, int n_tiles,
+                     const int* __restrict__ hist_scanned) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ int s_cnt[kWarps][kRadix];
+  __shared__ int s_base[kRadix];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
+  const int n_digits = (int)digit_mask + 1;
+  for (int d = threadIdx.x; d < n_digits; d += kSortThreads)
+    s_base[d] = hist_scanned[(long long)d * n_tiles + blockIdx.x];
+  __syncthreads();
+
+  const long long wbase = (long long)blockIdx.x * kSortTile + (long long)warp * (32 * kSortItems);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned key[kSortItems];
+  int val[kSortItems];
+  int rank[kSortItems];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    long long e = wbase + r * 32 + lane;
+    bool valid = e < n;
+    key[r] = valid ? keys_in[e] : 0u;
+    val[r] = valid ? vals_in[e] : 0;
+    int d = valid ? (int)((key[r] >> shift) & digit_mask) : kRadix;  // kRadix: own group
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int before = valid ? s_cnt[warp][d] : 0;
+    rank[r] = before + __popc(peers & lt_mask);
+    __syncwarp();
+    if (valid && (peers & lt_mask) == 0) s_cnt[warp][d] = before + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // Exclusive prefix over warps, per digit.
+  for (int d = threadIdx.x; d < n_digits; d += kSortThreads) {
+    int run = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      int c = s_cnt[w][d];
+      s_cnt[w][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    long long e = wbase + r * 32 + lane;
+    if (e < n) {
+      int d = (int)((key[r] >> shift) & digit_mask);
+      long long pos = (long long)s_base[d] + s_cnt[warp][d] + rank[r];
+      keys_out[pos] = key[r];
+      vals_out[pos] = val[r];
+    }
+  }
+}
+
+// seg_offsets[s] = first sorted position whose key >= s, for s in [0, n_segments].
+__global__ void seg_offsets_kernel(const unsigned* __restrict__ keys, long long n,
+                                   int n_segments, int* __restrict__ offsets) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j <= n;
+       j += (long long)gridDim.x * blockDim.x) {
+    long long lo = (j == 0) ? 0 : (long long)keys[j - 1] + 1;
+    long long hi = (j == n) ? n_segments : min((long long)keys[j], (long long)n_segments);
+    for (long long s = lo; s <= hi; ++s) offsets[s] = (int)j;
+  }
+}
+
+int grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  long long cap = (long long)sm_count() * 16;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+int sort_passes(int n_segments) {
+  unsigned maxkey = (unsigned)n_segments;  // sentinel key value
+  int bits = 0;
+  while (bits < 32 && (maxkey >> bits) != 0) ++bits;
+  if (bits == 0) bits = 1;
+  return (bits + kRadixBits - 1) / kRadixBits;
+}
+
+}  // namespace
+}  // namespace rubix
+
+using namespace rubix;
+
+extern "C" int rubix_aperture_mask(const float* coords, int64_t n, int64_t coord_stride,
+                                   const float* edges, int32_t n_edges, uint8_t* mask_out,
+                                   void* stream) {
+  RUBIX_REQUIRE(n >= 0, RUBIX_E_INVALID, "rubix_aperture_mask: n < 0");
+  RUBIX_REQUIRE(n_edges >= 1, RUBIX_E_SHAPE, "rubix_aperture_mask: need at least one edge");
+  RUBIX_REQUIRE(coord_stride >= 2, RUBIX_E_SHAPE, "rubix_aperture_mask: coord_stride < 2");
+  if (n == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(coords && edges && mask_out, RUBIX_E_INVALID,
+                "rubix_aperture_mask: null pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  aperture_mask_kernel<<<grid_for(n, 256), 256, 0, st>>>(coords, n, coord_stride, edges,
+                                                          n_edges, mask_out);
+  RUBIX_LAUNCH_CHECK("aperture_mask_kernel");
+  return RUBIX_OK;
+}
+
+extern "C" int rubix_spaxel_assign(const float* coords, int64_t n, int64_t coord_stride,
+                                   const float* edges, int32_t n_edges, int32_t* idx_out,
+                                   void* stream) {
+  RUBIX_REQUIRE(n >= 0, RUBIX_E_INVALID, "rubix_spaxel_assign: n < 0");
+  RUBIX_REQUIRE(n_edges >= 2, RUBIX_E_SHAPE, "rubix_spaxel_assign: need at least two edges");
+  RUBIX_REQUIRE((long long)(n_edges - 1) * (n_edges - 1) < (1LL << 31), RUBIX_E_SHAPE,
+                "rubix_spaxel_assign: (n_edges-1)^2 overflows int32");
+  RUBIX_REQUIRE(coord_stride >= 2, RUBIX_E_SHAPE, "rubix_spaxel_assign: coord_stride < 2");
+  if (n == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(coords && edges && idx_out, RUBIX_E_INVALID,
+                "rubix_spaxel_assign: null pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  size_t smem = n_edges <= kMaxSmemEdges ? (size_t)n_edges * sizeof(float) : 0;
+  spaxel_assign_kernel<<<grid_for(n, 256), 256, smem, st>>>(coords, n, coord_stride, edges,
+                                                             n_edges, idx_out);
+  RUBIX_LAUNCH_CHECK("spaxel_assign_kernel");
+  return RUBIX_OK;
+}
+
+extern "C" size_t rubix_spaxel_sort_workspace_size(int64_t n, int32_t n_segments) {
+  if (n < 0 || n_segments < 0) return 0;
+  long long n_tiles = (n + kSortTile - 1) / kSortTile;
+  if (n_tiles < 1) n_tiles = 1;
+  Carve c(nullptr);
+  c.take<unsigned>((size_t)n);               // keys A
+  c.take<unsigned>((size_t)n);               // keys B
+  c.take<int>((size_t)n);                    // vals scratch
+  c.take<int>((size_t)kRadix * n_tiles);     // histogram
+  return c.off;
+}
+
+extern "C" int rubix_spaxel_sort(const int32_t* idx, const uint8_t* keep, int64_t n,
+                                 int32_t n_segments, int32_t* perm_out,
+                                 int32_t* seg_offsets_out, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE,
+                "rubix_spaxel_sort: n must be in [0, 2^31)");
+  RUBIX_REQUIRE(n_segments >= 0 && n_segments < 0x7fffffff, RUBIX_E_SHAPE,
+                "rubix_spaxel_sort: bad n_segments");
+  RUBIX_REQUIRE(seg_offsets_out != nullptr, RUBIX_E_INVALID,
+                "rubix_spaxel_sort: seg_offsets_out is null");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n == 0) {
+    RUBIX_CUDA_TRY(cudaMemsetAsync(seg_offsets_out, 0, sizeof(int) * ((size_t)n_segments + 1), st));
+    return RUBIX_OK;
+  }
+  RUBIX_REQUIRE(idx && perm_out, RUBIX_E_INVALID, "rubix_spaxel_sort: null pointer");
+  size_t need = rubix_spaxel_sort_workspace_size(n, n_segments);
+  RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
+                "rubix_spaxel_sort: workspace of %zu bytes needed, %zu given", need,
+                workspace_bytes);
+  const int n_tiles = (int)((n + kSortTile - 1) / kSortTile);
+  Carve c(workspace);
+  unsigned* keys_a = c.take<unsigned>((size_t)n);
+  unsigned* keys_b = c.take<unsigned>((size_t)n);
+  int* vals_ws = c.take<int>((size_t)n);
+  int* hist = c.take<int>((size_t)kRadix * n_tiles);
+
+  const int passes = sort_passes(n_segments);
+  // The last pass must write into perm_out: pass p writes perm_out when
+  // (passes-1-p) is even, vals_ws otherwise.
+  auto dst_vals = [&](int p) { return ((passes - 1 - p) % 2 == 0) ? perm_out : vals_ws; };
+  int* vals_src = (dst_vals(0) == perm_out) ? vals_ws : perm_out;
+  make_keys_kernel<<<grid_for(n, 256), 256, 0, st>>>(idx, keep, n, n_segments, keys_a, vals_src);
+  RUBIX_LAUNCH_CHECK("make_keys_kernel");
+  unsigned* kin = keys_a;
+  unsigned* kout = keys_b;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = p * kRadixBits;
+    const unsigned dmask = (unsigned)(kRadix - 1);
+    int* vout = dst_vals(p);
+    radix_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, n, shift, dmask, n_tiles, hist);
+    RUBIX_LAUNCH_CHECK("radix_hist_kernel");
+    scan_exclusive_1block<<<1, 1024, 0, st>>>(hist, (long long)kRadix * n_tiles, 0);
+    RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
+    radix_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, vals_src, kout, vout, n, shift,
+                                                           dmask, n_tiles, hist);
+    RUBIX_LAUNCH_CHECK("radix_scatter_kernel");
+    unsigned* tk = kin;
+    kin = kout;
+    kout = tk;
+    vals_src = vout;
+  }
+  seg_offsets_kernel<<<grid_for(n + 1, 256), 256, 0, st>>>(kin, n, n_segments, seg_offsets_out);
+  RUBIX_LAUNCH_CHECK("seg_offsets_kernel");
+  return RUBIX_OK;
+}

@@ -1,0 +1,174 @@
+"""Torch-facing wrappers of the C ABI: one function per kernel entry point.
+
+Tensors must live on a CUDA device; they are passed to the library as raw device
+pointers together with the current torch stream.  Workspaces come from torch's
+caching allocator, so the library itself never allocates.  Every function raises
+(``ValueError`` for bad arguments, ``RubixError`` for a failing C-ABI call) and none
+has a CPU path.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+
+__all__ = [
+    "aperture_mask",
+    "spaxel_assign",
+    "spaxel_sort",
+    "cube_forward",
+    "psf_forward",
+    "lsf_forward",
+    "workspace",
+]
+
+
+def _stream(dev: torch.device) -> int:
+    return torch.cuda.current_stream(dev).cuda_stream
+
+
+def _check_cuda(name: str, t: torch.Tensor, dtype=None) -> None:
+    if not isinstance(t, torch.Tensor):
+        raise ValueError(f"{name} must be a torch.Tensor, got {type(t).__name__}")
+    if t.device.type != "cuda":
+        raise ValueError(f"{name} must be a CUDA tensor (rubix_gb300 has no CPU path)")
+    if dtype is not None and t.dtype != dtype:
+        raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+
+
+def _contig(name: str, t: torch.Tensor, dtype) -> torch.Tensor:
+    _check_cuda(name, t, None)
+    if t.dtype != dtype:
+        t = t.to(dtype)
+    return t.contiguous()
+
+
+def workspace(nbytes: int, device) -> torch.Tensor:
+    """A device scratch buffer of at least ``nbytes`` bytes (256-byte aligned)."""
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def aperture_mask(coords: torch.Tensor, edges: torch.Tensor) -> torch.Tensor:
+    """uint8 mask of particles inside [min(edges), max(edges)]^2 (x, y columns)."""
+    coords = _contig("coords", coords, torch.float32)
+    edges = _contig("edges", edges, torch.float32)
+    n = coords.shape[0]
+    out = torch.empty(n, dtype=torch.uint8, device=coords.device)
+    stride = coords.shape[1] if coords.dim() == 2 else 1
+    _lib.call("rubix_aperture_mask", _ptr(coords), n, stride, _ptr(edges), edges.numel(),
+              _ptr(out), _stream(coords.device))
+    return out
+
+
+def spaxel_assign(coords: torch.Tensor, edges: torch.Tensor) -> torch.Tensor:
+    """int32 flat spaxel index ix + nb*iy (square_spaxel_assignment semantics)."""
+    coords = _contig("coords", coords, torch.float32)
+    edges = _contig("edges", edges, torch.float32)
+    if coords.dim() != 2 or coords.shape[1] < 2:
+        raise ValueError(f"coords must be (n, >=2), got {tuple(coords.shape)}")
+    n = coords.shape[0]
+    out = torch.empty(n, dtype=torch.int32, device=coords.device)
+    _lib.call("rubix_spaxel_assign", _ptr(coords), n, coords.shape[1], _ptr(edges),
+              edges.numel(), _ptr(out), _stream(coords.device))
+    return out
+
+
+def spaxel_sort(idx: torch.Tensor, n_segments: int, keep: torch.Tensor | None = None):
+    """Stable sort by spaxel; returns (perm int32 [n], seg_offsets int32 [n_segments+1])."""
+    idx = _contig("idx", idx, torch.int32)
+    if keep is not None:
+        keep = _contig("keep", keep, torch.uint8)
+        if keep.numel() != idx.numel():
+            raise ValueError("keep must have one entry per particle")
+    n = idx.numel()
+    dev = idx.device
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+    offs = torch.empty(int(n_segments) + 1, dtype=torch.int32, device=dev)
+    nbytes = _lib.query("rubix_spaxel_sort_workspace_size", n, int(n_segments))
+    ws = workspace(nbytes, dev)
+    _lib.call("rubix_spaxel_sort", _ptr(idx), _ptr(keep), n, int(n_segments), _ptr(perm),
+              _ptr(offs), _ptr(ws), ws.numel(), _stream(dev))
+    return perm, offs
+
+
+def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, metallicity,
+                 age, velocity, vel_component, perm, seg_offsets, n_segments, out=None):
+    """Fused lookup + mass + Doppler/resample + per-spaxel sum -> cube [n_segments, L]."""
+    ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
+    if ssp_flux.dim() != 3:
+        raise ValueError("ssp_flux must be [n_met, n_age, n_wave]")
+    nz, na, nw = ssp_flux.shape
+    ssp_metallicity = _contig("ssp_metallicity", ssp_metallicity, torch.float32)
+    ssp_age = _contig("ssp_age", ssp_age, torch.float32)
+    ssp_wave_z = _contig("ssp_wave_z", ssp_wave_z, torch.float32)
+    wave_t = _contig("wave_t", wave_t, torch.float32)
+    if ssp_metallicity.numel() != nz or ssp_age.numel() != na or ssp_wave_z.numel() != nw:
+        raise ValueError("SSP grid sizes do not match ssp_flux")
+    mass = _contig("mass", mass, torch.float32).reshape(-1)
+    metallicity = _contig("metallicity", metallicity, torch.float32).reshape(-1)
+    age = _contig("age", age, torch.float32).reshape(-1)
+    velocity = _contig("velocity", velocity, torch.float32)
+    n = mass.numel()
+    if metallicity.numel() != n or age.numel() != n or velocity.shape[0] != n:
+        raise ValueError("particle arrays must all have the same length")
+    vstride = velocity.shape[1] if velocity.dim() == 2 else 1
+    perm = _contig("perm", perm, torch.int32)
+    seg_offsets = _contig("seg_offsets", seg_offsets, torch.int32)
+    L = wave_t.numel()
+    dev = mass.device
+    if out is None:
+        out = torch.empty((int(n_segments), L), dtype=torch.float32, device=dev)
+    else:
+        _check_cuda("out", out, torch.float32)
+        if out.dim() != 2 or out.shape[0] != n_segments or out.shape[1] < L or out.stride(1) != 1:
+            raise ValueError("out must be [n_segments, >=L] with unit stride along wavelength")
+    nbytes = _lib.query("rubix_cube_workspace_size", n, int(n_segments), L, nw)
+    ws = workspace(nbytes, dev)
+    _lib.call("rubix_cube_fwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
+              _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
+              _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
+              _ptr(seg_offsets), int(n_segments), n, _ptr(out), out.stride(0), _ptr(ws),
+              ws.numel(), _stream(dev))
+    return out
+
+
+def _host_taps(t) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(t, dtype=np.float32).reshape(-1))
+    return a
+
+
+def psf_forward(cube: torch.Tensor, taps_y, taps_x=None, out=None) -> torch.Tensor:
+    """Separable 'same' convolution of every wavelength plane of cube [ny, nx, L]."""
+    _check_cuda("cube", cube, torch.float32)
+    if cube.dim() != 3 or cube.stride(2) != 1 or cube.stride(0) != cube.shape[1] * cube.stride(1):
+        cube = cube.contiguous()
+    ny, nx, L = cube.shape
+    ty = _host_taps(taps_y)
+    tx = ty if taps_x is None else _host_taps(taps_x)
+    if out is None:
+        out = torch.empty((ny, nx, L), dtype=torch.float32, device=cube.device)
+    _lib.call("rubix_psf_fwd", _ptr(cube), _ptr(out), ny, nx, L, cube.stride(1), out.stride(1),
+              ty.ctypes.data, ty.size, tx.ctypes.data, tx.size, _stream(cube.device))
+    return out
+
+
+def lsf_forward(cube: torch.Tensor, taps, crop: int, out=None) -> torch.Tensor:
+    """Full 1-D convolution along the last axis cropped to [crop, L + crop)."""
+    _check_cuda("cube", cube, torch.float32)
+    if cube.stride(-1) != 1:
+        cube = cube.contiguous()
+    L = cube.shape[-1]
+    rows = cube.reshape(-1, L) if cube.is_contiguous() else cube.contiguous().reshape(-1, L)
+    k = _host_taps(taps)
+    if out is None:
+        out = torch.empty(cube.shape, dtype=torch.float32, device=cube.device)
+    orow = out.view(-1, L)
+    _lib.call("rubix_lsf_fwd", _ptr(rows), _ptr(orow), rows.shape[0], L, rows.stride(0),
+              orow.stride(0), k.ctypes.data, k.size, int(crop), _stream(cube.device))
+    return out
