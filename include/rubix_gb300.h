@@ -107,7 +107,7 @@ RUBIX_API int rubix_spaxel_sort(const int32_t* idx, const uint8_t* keep, int64_t
  *   perm, seg_offsets   output of rubix_spaxel_sort for n_segments spaxels
  */
 RUBIX_API size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
-                                 int32_t n_wave);
+                                           int32_t n_met, int32_t n_age, int32_t n_wave);
 
 /*
  * cube[s][0..n_wave_t) = sum over kept particles p of spaxel s of
@@ -117,7 +117,13 @@ RUBIX_API size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32_
  * (core/ifu.py:226-295, spectra/ifu.py:168-266) and calculate_datacube
  * (core/ifu.py:299-341, spectra/ifu.py:270-288), fused; no N x lambda array is
  * materialised.  Deterministic: the same inputs give bit-identical cubes.
- * n_wave_t <= 4096.
+ * With n_lsf_taps > 0 (lsf_taps a HOST array of <= 63 taps) every finished
+ * spectrum is also convolved along wavelength exactly as rubix_lsf_fwd does with
+ * (lsf_taps, n_lsf_taps, lsf_crop); LSF and PSF act on different axes and commute,
+ * so a pipeline may fuse its LSF step here and run the PSF afterwards.
+ * Limits: n_wave_t <= 4096; n_wave up to about 2600 (shared-memory rows).
+ * The workspace (256-byte aligned) must not be shared by calls in flight at the
+ * same time.
  */
 RUBIX_API int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,
                    const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
@@ -125,8 +131,16 @@ RUBIX_API int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity
                    const float* mass, const float* metallicity, const float* age,
                    const float* velocity, int64_t vel_stride, int32_t vel_component,
                    const int32_t* perm, const int32_t* seg_offsets, int32_t n_segments,
-                   int64_t n, float* cube, int64_t spaxel_stride, void* workspace,
+                   int64_t n, const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
+                   float* cube, int64_t spaxel_stride, void* workspace,
                    size_t workspace_bytes, void* stream);
+
+/*
+ * Reads the device error word of the last rubix_cube_fwd that used `workspace`
+ * (synchronises `stream`).  *device_error = 1 and RUBIX_E_DEVICE if a shared-memory
+ * copy wait in the kernel timed out (the cube is then invalid), else 0 / RUBIX_OK.
+ */
+RUBIX_API int rubix_cube_status(const void* workspace, int* device_error, void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* (c) PSF: per-wavelength 2-D convolution, separable Gaussian               */
@@ -135,7 +149,7 @@ RUBIX_API int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity
 /*
  * out[y][x][l] = sum_{i,j} ty[i] tx[j] in[y + oy - i][x + ox - j][l] with zero
  * padding, oy = (m_y-1)/2, ox = (m_x-1)/2 ("same" mode of convolve2d).  ty/tx are
- * HOST arrays of m_y/m_x taps (m_y, m_x <= 63).  With ty = tx = the normalised 1-D
+ * HOST arrays of m_y/m_x taps (m_y <= 31, m_x <= 63).  With ty = tx = the normalised 1-D
  * Gaussian this equals convolve2d(plane, gaussian_kernel_2d, mode="same") for every
  * plane: apply_psf, rubix/telescope/psf/psf.py:33-58 with kernels.py:5-31 (step
  * convolve_psf, rubix/core/psf.py:15-75).  in and out must not overlap.

@@ -38,12 +38,13 @@ SIGNATURES = {
     "rubix_spaxel_assign": (_c.c_int, [_vp, _i64, _i64, _vp, _i32, _vp, _vp]),
     "rubix_spaxel_sort_workspace_size": (_sz, [_i64, _i32]),
     "rubix_spaxel_sort": (_c.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _sz, _vp]),
-    "rubix_cube_workspace_size": (_sz, [_i64, _i32, _i32, _i32]),
+    "rubix_cube_workspace_size": (_sz, [_i64, _i32, _i32, _i32, _i32, _i32]),
+    "rubix_cube_status": (_c.c_int, [_vp, _c.POINTER(_c.c_int), _vp]),
     "rubix_cube_fwd": (
         _c.c_int,
         [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32,
          _vp, _vp, _vp, _vp, _i64, _i32,
-         _vp, _vp, _i32, _i64, _vp, _i64, _vp, _sz, _vp],
+         _vp, _vp, _i32, _i64, _vp, _i32, _i32, _vp, _i64, _vp, _sz, _vp],
     ),
     "rubix_psf_fwd": (
         _c.c_int, [_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _vp, _i32, _vp]

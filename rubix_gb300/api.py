@@ -1,0 +1,130 @@
+"""Device-resident renderer for the particle -> datacube path.
+
+``IFURenderer`` holds the per-configuration constants on the GPU (SSP template grid,
+redshifted SSP wavelengths, telescope wavelength grid, spatial bin edges, PSF and
+LSF taps) and runs the kernels of the C ABI for one set of particles:
+
+    aperture mask -> spaxel assignment -> stable sort by spaxel
+    -> fused lookup/mass/Doppler/resample/accumulate -> PSF -> LSF
+
+It is the engine behind the rubix-compatible step functions in ``rubix_gb300.core``
+(where each step stays separately callable) and the one-call path used for
+benchmarks.  Inputs may be host (numpy / CPU tensors, copied once) or CUDA tensors.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import ops
+from . import telescope as tel
+
+
+def _dev(a, device, dtype=torch.float32):
+    if isinstance(a, torch.Tensor):
+        t = a
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(a))
+    if t.dtype != dtype:
+        t = t.to(dtype)
+    if t.device != torch.device(device):
+        t = t.to(device, non_blocking=True)
+    return t.contiguous()
+
+
+@dataclass
+class CubeStages:
+    pixel_assignment: torch.Tensor
+    mask: Optional[torch.Tensor]
+    perm: torch.Tensor
+    seg_offsets: torch.Tensor
+    cube: torch.Tensor             # output of the accumulate kernel [sbin, sbin, L]
+    cube_psf: Optional[torch.Tensor]
+    cube_lsf: Optional[torch.Tensor]
+    lsf_fused: bool = False        # cube already holds the LSF (applied before the PSF)
+    final: Optional[torch.Tensor] = None
+
+
+class IFURenderer:
+    """Constants of one (SSP, telescope, redshift, PSF, LSF) configuration on a device."""
+
+    def __init__(self, ssp_age, ssp_metallicity, ssp_wavelength, ssp_flux, wave_t, edges,
+                 sbin: int, dist_z: float, psf_taps=None, lsf_taps=None, lsf_crop: int = 12,
+                 velocity_axis: int = 2, apply_filter: bool = True, device="cuda"):
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("IFURenderer needs a CUDA device (rubix_gb300 has no CPU path)")
+        self.ssp_age = _dev(ssp_age, self.device)
+        self.ssp_metallicity = _dev(ssp_metallicity, self.device)
+        flux = np.asarray(ssp_flux, dtype=np.float32) if not isinstance(ssp_flux, torch.Tensor) else ssp_flux
+        self.ssp_flux = _dev(flux, self.device)
+        wz = tel.cosmological_doppler_shift(dist_z, np.asarray(ssp_wavelength, dtype=np.float32)
+                                            if not isinstance(ssp_wavelength, torch.Tensor)
+                                            else ssp_wavelength.cpu().numpy())
+        self.ssp_wave_z = _dev(wz, self.device)
+        self.wave_t = _dev(wave_t, self.device)
+        self.edges = _dev(edges, self.device)
+        self.sbin = int(sbin)
+        self.n_wave_t = int(self.wave_t.numel())
+        self.psf_taps = None if psf_taps is None else np.asarray(psf_taps, dtype=np.float64)
+        self.lsf_taps = None if lsf_taps is None else np.asarray(lsf_taps, dtype=np.float64)
+        self.lsf_crop = int(lsf_crop)
+        self.velocity_axis = int(velocity_axis)
+        self.apply_filter = bool(apply_filter)
+
+    @classmethod
+    def from_workload(cls, w, device="cuda", psf=True, lsf=True):
+        return cls(w.ssp.age, w.ssp.metallicity, w.ssp.wavelength, w.ssp.flux, w.wave_t, w.edges,
+                   w.sbin, w.dist_z,
+                   psf_taps=tel.gaussian_taps_1d(w.psf_size, w.psf_sigma) if psf else None,
+                   lsf_taps=tel.lsf_taps(w.lsf_sigma, w.wave_res) if lsf else None,
+                   device=device)
+
+    # -------------------------------------------------------------- steps
+    def assign(self, coords):
+        coords = _dev(coords, self.device)
+        idx = ops.spaxel_assign(coords, self.edges)
+        mask = ops.aperture_mask(coords, self.edges) if self.apply_filter else None
+        return idx, mask
+
+    def sort(self, idx, mask=None):
+        return ops.spaxel_sort(idx, self.sbin * self.sbin, mask)
+
+    def accumulate(self, mass, metallicity, age, velocity, perm, seg_offsets, out=None,
+                   with_lsf=False):
+        """Fused lookup/mass/Doppler/resample/sum; ``with_lsf`` adds the LSF epilogue."""
+        cube = ops.cube_forward(self.ssp_flux, self.ssp_metallicity, self.ssp_age, self.ssp_wave_z,
+                                self.wave_t, _dev(mass, self.device), _dev(metallicity, self.device),
+                                _dev(age, self.device), _dev(velocity, self.device),
+                                self.velocity_axis, perm, seg_offsets, self.sbin * self.sbin, out=out,
+                                lsf_taps=self.lsf_taps if with_lsf else None,
+                                lsf_crop=self.lsf_crop)
+        return cube.view(self.sbin, self.sbin, self.n_wave_t)
+
+    def psf(self, cube, out=None):
+        return ops.psf_forward(cube, self.psf_taps, out=out)
+
+    def lsf(self, cube, out=None):
+        return ops.lsf_forward(cube, self.lsf_taps, self.lsf_crop, out=out)
+
+    # -------------------------------------------------------------- whole path
+    def render(self, coords, velocity, mass, metallicity, age, fuse_lsf=True) -> CubeStages:
+        """Whole path.  With ``fuse_lsf`` the LSF runs inside the accumulate kernel and the
+        PSF afterwards (the two act on different axes and commute), saving one read and
+        one write of the cube; the final cube is the same."""
+        idx, mask = self.assign(coords)
+        perm, offs = self.sort(idx, mask)
+        fuse = fuse_lsf and self.lsf_taps is not None
+        cube = self.accumulate(mass, metallicity, age, velocity, perm, offs, with_lsf=fuse)
+        if fuse:
+            c_psf = self.psf(cube) if self.psf_taps is not None else None
+            final = c_psf if c_psf is not None else cube
+            return CubeStages(idx, mask, perm, offs, cube, c_psf, None, True, final)
+        c_psf = self.psf(cube) if self.psf_taps is not None else None
+        c_lsf = self.lsf(c_psf if c_psf is not None else cube) if self.lsf_taps is not None else None
+        final = c_lsf if c_lsf is not None else (c_psf if c_psf is not None else cube)
+        return CubeStages(idx, mask, perm, offs, cube, c_psf, c_lsf, False, final)

@@ -3,53 +3,68 @@
 // per-spaxel accumulation of the datacube.
 //
 // Work decomposition
-//   * Particles arrive sorted by spaxel (kernel (a)).  A setup pass gathers each
-//     particle into a 32-byte record (mass, Doppler factor, interpolation cell and
-//     weights, first/last SSP bracket of the telescope range).
-//   * Work items are (spaxel, chunk of <= kChunk particles).  A persistent kernel
-//     pulls items from an atomic counter.  A block of 256 threads owns the whole
-//     telescope grid of its spaxel: thread `tid` holds t = tid + 256*r, r < R, in
-//     registers (wavelength, bin width, bucket coordinate, accumulator).
-//   * Per batch of kPB particles the block builds, in shared memory, the particle's
-//     mixed template row restricted to the telescope range: entry k holds
-//     (lambda'_k, slope_k, G_k, lambda'_{k+1}) with lambda'_k = fl32(lambda_z,k *
-//     fl32(exp(v/c))) -- the float32 grid rubix materialises -- and the in-range
-//     flux sum T.  Each thread then interpolates its R wavelengths (bracket from a
-//     log-wavelength bucket table, corrected by exact comparisons on lambda'),
-//     keeps the values in registers and sums T' = sum_t I_t dlambda_t.  One block
-//     reduction per batch gives s = nan_to_num(T/T'), and the accumulators take
-//     mass * s * I.  No particle spectrum is ever written to memory.
+//   * Setup passes (a few microseconds): a bucket table over log wavelength, the
+//     "corner table" holding, for every (metallicity, age) cell of the SSP grid and
+//     every SSP wavelength, the four corner fluxes of the cell as one float4, and a
+//     gather of the spaxel-sorted particles into 32-byte records (mass, Doppler factor
+//     alpha = fl32(exp(v/c)), cell and bilinear weights, and the SSP brackets
+//     kstart/kend of both ends of the telescope range on the particle's float32 grid
+//     lambda'_k = fl32(lambda_z,k * alpha)).
+//   * Work items are (spaxel, chunk of <= kChunk particles), largest first, pulled by a
+//     persistent kernel from an atomic counter.  A block of 256 threads owns the
+//     telescope grid of its spaxel: thread i holds R consecutive wavelengths
+//     t = i*R + r in registers (wavelength, bin width, accumulator).
+//   * Per batch of kPB particles one thread issues a 1-D TMA bulk copy of each
+//     particle's corner-table segment (its bracket range only) into shared memory; it
+//     completes on an mbarrier while the block evaluates the previous batch.  The block
+//     then builds per particle the row of entries (lambda'_k, slope_k, G_k,
+//     lambda'_{k+1}) of the mixed template G = sum_c w_c F_c and the in-range flux sum T
+//     (rubix/spectra/ifu.py:241-245).
+//   * Evaluation: each thread finds the exact bracket of its first wavelength (bucket
+//     table + exact comparisons on lambda') and walks forward over its R wavelengths;
+//     when every SSP interval is wider than every telescope bin the walk advances at
+//     most once per wavelength (one predicated load).  Interpolated values stay in
+//     registers while T' = sum_t I_t dlambda_t is reduced over the block; then
+//     s = nan_to_num(T/T') and the accumulators take mass * s * I.
 //   * Spaxels with more than kChunk particles are split; each chunk writes a partial
-//     spectrum to the workspace and the last chunk to finish sums the partials in
-//     chunk order (Kahan), so the cube is bit-reproducible with no float atomics.
+//     spectrum to the workspace and the last chunk to finish sums the partials in chunk
+//     order (Kahan).  No float atomics: results are bit-reproducible.
+//   * Optional epilogue: the LSF convolution along wavelength of the finished spectrum
+//     (rubix/telescope/lsf/lsf.py:29-105), which commutes with the PSF.
 #include "common.cuh"
 #include "scan.cuh"
+#include "tma.cuh"
 
 namespace rubix {
 namespace {
 
 constexpr int kAccThreads = 256;
 constexpr int kAccWarps = kAccThreads / 32;
-constexpr int kPB = 2;          // particles per batch
-constexpr int kChunk = 512;     // particles per work item
-constexpr int kBuckets = 2048;  // log-wavelength bucket table entries
-constexpr double kVmaxKms = 10000.0;  // bucket table sized for |v| <= 10^4 km/s
-constexpr int kMaxWaveT = kAccThreads * 16;
+constexpr int kPB = 2;          // particles per batch (the block reduction packs 2x2 values)
+constexpr int kChunk = 256;     // particles per work item
+constexpr int kBigItem = 64;    // single-chunk spaxels with at least this many go first
+constexpr int kBuckets = 1024;  // log-wavelength bucket table entries
+constexpr double kVmaxKms = 10000.0;  // bucket table and one-step-walk check sized for this
+constexpr int kMaxR = 16;
+constexpr int kMaxWaveT = kAccThreads * kMaxR;
+constexpr int kGenericFlag = 1 << 30;  // in rec.b.z: particle needs the general walk
+constexpr int kMaxLsfTaps = 63;
 
 struct CubeCtrl {
   int next_item;
   int n_items;
-  int error;
+  int error;               // 1: a TMA wait timed out
+  unsigned dz_min_bits;    // min SSP spacing near the telescope range (float bits)
+  unsigned dt_max_bits;    // max telescope bin width (float bits)
   int pad0;
-  double lnq0;   // log of the lowest wavelength covered by bucket 0
-  double h;      // bucket width in log wavelength
-  float bmax;    // |B| clamp in bucket units
-  float pad1[3];
+  double lnq0;             // log of the lowest wavelength covered by bucket 0
+  double h;                // bucket width in log wavelength
 };
 
-struct ParticleRec {  // 32 bytes, two vector loads
-  float4 a;  // mass, alpha = fl32(exp(v/c)), B = (v/c)/h (bucket units), tz
-  int4 b;    // cell (lower corner iz*nA+ia, -1 if outside), kstart, kend, ta bits
+struct ParticleRec {  // 48 bytes, three vector loads
+  float4 a;  // mass, alpha, B = (v/c)/h in bucket units, tz
+  int4 b;    // cell (iz*(nA-1)+ia, -1 outside the grid), kstart, kend|flags, ta bits
+  float4 c;  // T = in-range flux sum of the mixed template, unused x3
 };
 
 __device__ __forceinline__ int count_le_scaled(const float* __restrict__ wz, int n, float alpha,
@@ -72,42 +87,98 @@ __device__ __forceinline__ int count_le(const float* __restrict__ g, int n, floa
   return lo;
 }
 
-// Bucket table over log(q) and per-wavelength bucket coordinates A_t.
+__device__ __forceinline__ void bucket_params(const float* wave_t, int n_t, double& lnq0,
+                                              double& h) {
+  const double c = kSpeedOfLight;
+  lnq0 = log((double)wave_t[0]) - kVmaxKms / c;
+  const double hi = log((double)wave_t[n_t - 1]) + kVmaxKms / c;
+  h = (hi - lnq0) / (double)(kBuckets - 2);
+  if (!(h > 0.0)) h = 1e-6;
+}
+
+// Bucket table over log(q), per-wavelength bucket coordinates A_t, and the spacing
+// extrema that decide whether the one-step walk is exact.  Any number of blocks;
+// ctrl->dz_min_bits / dt_max_bits must be preset to 0xffffffff / 0.
 __global__ void cube_setup_kernel(const float* __restrict__ wave_z, int n_wave,
                                   const float* __restrict__ wave_t, int n_t,
                                   CubeCtrl* __restrict__ ctrl, float* __restrict__ At,
                                   int2* __restrict__ bucket) {
-  __shared__ double s_lnq0, s_h;
-  if (threadIdx.x == 0) {
-    const double c = kSpeedOfLight;
-    double lo = log((double)wave_t[0]) - kVmaxKms / c;
-    double hi = log((double)wave_t[n_t - 1]) + kVmaxKms / c;
-    double h = (hi - lo) / (double)(kBuckets - 2);
-    if (!(h > 0.0)) h = 1e-6;
-    s_lnq0 = lo;
-    s_h = h;
+  double lnq0, h;
+  bucket_params(wave_t, n_t, lnq0, h);
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gsz = gridDim.x * blockDim.x;
+  if (gtid == 0) {
     ctrl->next_item = 0;
     ctrl->error = 0;
-    ctrl->lnq0 = lo;
+    ctrl->lnq0 = lnq0;
     ctrl->h = h;
-    ctrl->bmax = (float)((kVmaxKms / c) / h);
   }
-  __syncthreads();
-  const double lnq0 = s_lnq0, h = s_h;
-  for (int t = threadIdx.x; t < n_t; t += blockDim.x)
+  for (int t = gtid; t < n_t; t += gsz) {
     At[t] = (float)((log((double)wave_t[t]) - lnq0) / h);
-  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) {
+    if (t > 0) {
+      float d = wave_t[t] - wave_t[t - 1];
+      if (!(d >= 0.f)) d = 3.0e38f;  // non-ascending grid: disable the one-step walk
+      atomicMax(&ctrl->dt_max_bits, __float_as_uint(d));
+    }
+  }
+  // SSP spacing over the wavelengths any particle with |v| <= vmax can bracket.
+  const double qlo = exp(lnq0) * 0.999, qhi = exp(lnq0 + (kBuckets - 2) * h) * 1.001;
+  for (int k = gtid; k + 1 < n_wave; k += gsz) {
+    const double a = wave_z[k], b = wave_z[k + 1];
+    if (b >= qlo && a <= qhi) {
+      float d = wave_z[k + 1] - wave_z[k];
+      if (!(d > 0.f)) d = 0.f;
+      atomicMin(&ctrl->dz_min_bits, __float_as_uint(d));
+    }
+  }
+  for (int b = gtid; b < kBuckets; b += gsz) {
     // Bucket b covers u in [b - 0.5, b + 0.5) (round-to-nearest lookup).
-    double q = exp(lnq0 + ((double)b - 0.5) * h);
+    const double q = exp(lnq0 + ((double)b - 0.5) * h);
     int lo = 0, hi = n_wave;
     while (lo < hi) {
       int mid = (lo + hi) >> 1;
       if ((double)wave_z[mid] <= q) lo = mid + 1; else hi = mid;
     }
-    int k0 = lo - 1;
+    const int k0 = lo - 1;
     float thr = 3.0e38f;
     if (k0 + 1 < n_wave) thr = (float)((log((double)wave_z[k0 + 1]) - lnq0) / h);
     bucket[b] = make_int2(k0, __float_as_int(thr));
+  }
+}
+
+// Corner table: ct[(iz*(nA-1) + ia)*nW + k] = (F[iz][ia][k], F[iz+1][ia][k],
+// F[iz][ia+1][k], F[iz+1][ia+1][k]).
+__global__ void cube_corner_table_kernel(const float* __restrict__ flux, int nZ, int nA,
+                                         int nW, float4* __restrict__ ct) {
+  const long long total = (long long)(nZ - 1) * (nA - 1) * nW;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long cell = i / nW;
+    const int k = (int)(i - cell * nW);
+    const int iz = (int)(cell / (nA - 1)), ia = (int)(cell - (long long)iz * (nA - 1));
+    const long long b00 = ((long long)iz * nA + ia) * nW + k;
+    const long long b10 = b00 + (long long)nA * nW;
+    ct[i] = make_float4(flux[b00], flux[b10], flux[b00 + nW], flux[b10 + nW]);
+  }
+}
+
+// prefix[r][k] = sum_{k'=1..k} F[r][k'] * (lambda_z,k' - lambda_z,k'-1) for every SSP row
+// r (float64), prefix[r][0] = 0.  With it the in-range flux sum of a particle,
+// T = sum_{k in mask} G_k (lambda'_k - lambda'_{k-1}) (rubix/spectra/ifu.py:241-245),
+// is alpha * sum_c w_c (prefix[c][kb] - prefix[c][ka-1]): the float32 rounding of
+// lambda'_k = fl32(lambda_z,k * alpha) enters that sum only through telescoping
+// differences, ~1e-7 relative.
+__global__ void cube_prefix_kernel(const float* __restrict__ flux, int rows, int nW,
+                                   const float* __restrict__ wave_z, double* __restrict__ prefix) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+    const float* f = flux + (long long)r * nW;
+    double* o = prefix + (long long)r * nW;
+    double acc = 0.0;
+    o[0] = 0.0;
+    for (int k = 1; k < nW; ++k) {
+      acc += (double)f[k] * (double)(wave_z[k] - wave_z[k - 1]);
+      o[k] = acc;
+    }
   }
 }
 
@@ -119,71 +190,104 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
                                    const float* __restrict__ ag, int nA,
                                    const float* __restrict__ wave_z, int n_wave,
                                    const float* __restrict__ wave_t, int n_t,
+                                   const double* __restrict__ prefix,
                                    const CubeCtrl* __restrict__ ctrl,
                                    ParticleRec* __restrict__ rec) {
   const long long n_valid = seg_off[n_seg];
   const float t_lo = wave_t[0], t_hi = wave_t[n_t - 1];
   const double h = ctrl->h;
-  const float bmax = ctrl->bmax;
+  const double vmc = kVmaxKms / kSpeedOfLight;
+  const float bmax = (float)(vmc / h);
+  const float alo = (float)exp(-vmc), ahi = (float)exp(vmc);
+  // lambda' spacing >= alpha*dz minus two float32 roundings of lambda' (|lambda'| < 2^14)
+  const float dz = __uint_as_float(ctrl->dz_min_bits), dt = __uint_as_float(ctrl->dt_max_bits);
+  const bool coarse_ok = dz * alo - 4.0e-3f > dt;
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n && j < n_valid;
        j += (long long)gridDim.x * blockDim.x) {
     const long long i = perm[j];
     const float Z = met[i], A = age[i], m = mass[i];
     const float v = vel[i * vel_stride + vel_comp];
     // interpax.interp2d(method="linear"): cell from searchsorted(side='right').
-    int iz = min(max(count_le(zg, nZ, Z), 1), nZ - 1);
-    int ia = min(max(count_le(ag, nA, A), 1), nA - 1);
-    float dz = zg[iz] - zg[iz - 1], da = ag[ia] - ag[ia - 1];
-    float tz = dz == 0.f ? 0.f : (Z - zg[iz - 1]) / dz;
-    float ta = da == 0.f ? 0.f : (A - ag[ia - 1]) / da;
-    bool outside = (Z < zg[0]) || (Z > zg[nZ - 1]) || (A < ag[0]) || (A > ag[nA - 1]);
-    int cell = outside ? -1 : (iz - 1) * nA + (ia - 1);
+    const int iz = min(max(count_le(zg, nZ, Z), 1), nZ - 1);
+    const int ia = min(max(count_le(ag, nA, A), 1), nA - 1);
+    const float dzg = zg[iz] - zg[iz - 1], dag = ag[ia] - ag[ia - 1];
+    const float tz = dzg == 0.f ? 0.f : (Z - zg[iz - 1]) / dzg;
+    const float ta = dag == 0.f ? 0.f : (A - ag[ia - 1]) / dag;
+    const bool outside = (Z < zg[0]) || (Z > zg[nZ - 1]) || (A < ag[0]) || (A > ag[nA - 1]);
+    const int cell = outside ? -1 : (iz - 1) * (nA - 1) + (ia - 1);
     const double vc = (double)v / kSpeedOfLight;
     const float alpha = (float)exp(vc);
     float B = (float)(vc / h);
     B = fminf(fmaxf(B, -bmax), bmax);
-    int ks = count_le_scaled(wave_z, n_wave, alpha, t_lo) - 1;
+    const int ks = count_le_scaled(wave_z, n_wave, alpha, t_lo) - 1;
     int ke = count_le_scaled(wave_z, n_wave, alpha, t_hi) - 1;
     ke = max(ke, ks);  // keeps the shared-memory row non-empty for any input grid
+    const bool coarse = coarse_ok && alpha >= alo && alpha <= ahi;
+    // In-range flux sum T: entries ka..kb with t_lo <= lambda'_k <= t_hi, k >= 1.
+    double T = 0.0;
+    if (cell >= 0) {
+      int ka = (ks >= 0 && __fmul_rn(wave_z[ks], alpha) >= t_lo) ? ks : ks + 1;
+      ka = max(ka, 1);
+      const int kb = min(count_le_scaled(wave_z, n_wave, alpha, t_hi) - 1, n_wave - 1);
+      if (ka <= kb) {
+        const long long r00 = (long long)(iz - 1) * nA + (ia - 1);
+        const long long rr[4] = {r00, r00 + nA, r00 + 1, r00 + nA + 1};  // 00, 10, 01, 11
+        const double w[4] = {(1.0 - tz) * (1.0 - ta), (double)tz * (1.0 - ta),
+                             (1.0 - tz) * (double)ta, (double)tz * ta};
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          T += w[c] * (prefix[rr[c] * n_wave + kb] - prefix[rr[c] * n_wave + ka - 1]);
+        T *= (double)alpha;
+      }
+    }
     ParticleRec r;
     r.a = make_float4(m, alpha, B, tz);
-    r.b = make_int4(cell, ks, ke, __float_as_int(ta));
+    r.b = make_int4(cell, ks, ke | (coarse ? 0 : kGenericFlag), __float_as_int(ta));
+    r.c = make_float4((float)T, 0.f, 0.f, 0.f);
     rec[j] = r;
   }
 }
 
-// Per spaxel: number of chunks; multi-chunk spaxels get slots, the others a flag.
+// Per spaxel: chunk count.  Multi-chunk spaxels get one item (and partial slot) per
+// chunk; single-chunk spaxels are split into a "big" and a "small" class.
 __global__ void cube_count_kernel(const int* __restrict__ seg_off, int n_seg,
-                                  int* __restrict__ slot_cnt, int* __restrict__ single_cnt) {
+                                  int* __restrict__ slot_cnt, int* __restrict__ big_cnt,
+                                  int* __restrict__ small_cnt) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_seg; s += gridDim.x * blockDim.x) {
-    int cnt = seg_off[s + 1] - seg_off[s];
-    int nch = cnt <= kChunk ? 1 : (cnt + kChunk - 1) / kChunk;
+    const int cnt = seg_off[s + 1] - seg_off[s];
+    const int nch = cnt <= kChunk ? 1 : (cnt + kChunk - 1) / kChunk;
     slot_cnt[s] = nch > 1 ? nch : 0;
-    single_cnt[s] = nch > 1 ? 0 : 1;
+    big_cnt[s] = (nch == 1 && cnt >= kBigItem) ? 1 : 0;
+    small_cnt[s] = (nch == 1 && cnt < kBigItem) ? 1 : 0;
   }
 }
 
-// Items [0, total_slots) are the chunks of multi-chunk spaxels (item = partial slot),
-// then one item per single-chunk spaxel.
+// Item order: chunks of multi-chunk spaxels (item index = partial slot), then big
+// single-chunk spaxels, then the rest.
 __global__ void cube_fill_items_kernel(const int* __restrict__ seg_off, int n_seg,
                                        const int* __restrict__ slot_start,
-                                       const int* __restrict__ single_start,
+                                       const int* __restrict__ big_start,
+                                       const int* __restrict__ small_start,
                                        int2* __restrict__ items, CubeCtrl* __restrict__ ctrl) {
   const int total_slots = slot_start[n_seg];
+  const int total_big = big_start[n_seg];
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_seg; s += gridDim.x * blockDim.x) {
-    int cnt = seg_off[s + 1] - seg_off[s];
+    const int cnt = seg_off[s + 1] - seg_off[s];
     if (cnt > kChunk) {
-      int nch = (cnt + kChunk - 1) / kChunk;
+      const int nch = (cnt + kChunk - 1) / kChunk;
       for (int c = 0; c < nch; ++c) items[slot_start[s] + c] = make_int2(s, c);
+    } else if (cnt >= kBigItem) {
+      items[total_slots + big_start[s]] = make_int2(s, 0);
     } else {
-      items[total_slots + single_start[s]] = make_int2(s, 0);
+      items[total_slots + total_big + small_start[s]] = make_int2(s, 0);
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->n_items = total_slots + single_start[n_seg];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    ctrl->n_items = total_slots + total_big + small_start[n_seg];
 }
 
 struct MainArgs {
-  const float* flux;
+  const float4* ct;  // corner table [(nZ-1)*(nA-1)][nW]
   const float* wave_z;
   int nZ, nA, n_wave;
   const float* wave_t;
@@ -200,109 +304,260 @@ struct MainArgs {
   CubeCtrl* ctrl;
   const int2* bucket;
   int row_cap;
+  int lsf_k, lsf_crop;  // lsf_k = 0: no LSF epilogue
+  float lsf[kMaxLsfTaps + 1];
 };
 
-struct alignas(16) BatchMeta {
-  int ks[kPB];
-  int ke[kPB];
-  float B[kPB];
+// Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned).
+struct SmemLayout {
+  size_t wz, bucket, stage, rows, red, rec, total;
 };
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+__host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
+  SmemLayout L;
+  size_t o = 0;
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  L.wz = o;     o = al(o + sizeof(float) * n_wave);
+  L.bucket = o; o = al(o + sizeof(int2) * kBuckets);
+  L.stage = o;  o = al(o + sizeof(float4) * kPB * (size_t)row_cap);
+  L.rows = o;   // also holds the zero-padded spectrum of the LSF epilogue
+  o = al(o + std::max(sizeof(float4) * kPB * (size_t)row_cap,
+                      sizeof(float) * (size_t)(kMaxWaveT + 2 * kMaxLsfTaps + 8)));
+  L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 2);
+  L.rec = o;    o = al(o + sizeof(ParticleRec) * kChunk);
+  L.total = o;
+  return L;
 }
 
-// Builds the shared-memory rows of particles [j0, j0+cnt) and writes each
-// particle's partial in-range flux sums T into red[.].x.
-__device__ __forceinline__ void build_rows(const MainArgs& a, long long j0, int cnt,
-                                           float4* __restrict__ rows, BatchMeta* meta,
-                                           float2* red, float* red_m, int lane, int warp) {
-  const float t_lo = a.wave_t[0], t_hi = a.wave_t[a.n_t - 1];
-  const int nW = a.n_wave;
-  for (int p = 0; p < cnt; ++p) {
-    const ParticleRec r = a.rec[j0 + p];
-    const float m = r.a.x, alpha = r.a.y, tz = r.a.w;
-    const int cell = r.b.x, ks = r.b.y, ke = r.b.z;
-    const float ta = __int_as_float(r.b.w);
-    if (threadIdx.x == 0) {
-      meta->ks[p] = ks;
-      meta->ke[p] = ke;
-      meta->B[p] = r.a.z;
-      red_m[p] = m;
+// Thread 0: arm the barrier and issue one bulk copy per particle of the batch: the
+// corner-table entries k in [max(kstart,0), min(kend+1, nW-1)] of its cell.
+__device__ __forceinline__ void issue_stage(const MainArgs& a, const ParticleRec* recs, int cnt,
+                                            float4* stage, uint64_t* bar) {
+  fence_proxy_async_smem();  // earlier generic reads of the staging buffer come first
+  uint32_t bytes = 0;
+  int klo[kPB], nk[kPB], cells[kPB];
+#pragma unroll
+  for (int p = 0; p < kPB; ++p) {
+    cells[p] = -1;
+    klo[p] = 0;
+    nk[p] = 0;
+    if (p < cnt) {
+      const int4 b = recs[p].b;
+      const int ks = b.y, ke = b.z & ~kGenericFlag;
+      klo[p] = max(ks, 0);
+      nk[p] = min(ke + 1, a.n_wave - 1) - klo[p] + 1;
+      cells[p] = b.x;
+      if (b.x >= 0) bytes += 16u * (uint32_t)nk[p];
     }
-    const float w00 = (1.f - tz) * (1.f - ta), w10 = tz * (1.f - ta);
-    const float w01 = (1.f - tz) * ta, w11 = tz * ta;
-    const float* f00 = a.flux + (long long)(cell < 0 ? 0 : cell) * nW;
-    const float* f10 = f00 + (long long)a.nA * nW;
-    const float* f01 = f00 + nW;
-    const float* f11 = f10 + nW;
-    float4* row = rows + p * a.row_cap;
-    const int n_e = ke - ks + 1;
-    float tsum = 0.f;
-    for (int base = warp * 31; base < n_e; base += kAccWarps * 31) {
-      const int e = base + lane;
-      const int k = ks + e;  // in [-1, nW]
-      float lp, G;
-      {
-        const int kk = min(max(k, 0), nW - 1);
-        G = 0.f;
-        if (cell >= 0) {
-          G = w00 * __ldg(f00 + kk);
-          G = fmaf(w10, __ldg(f10 + kk), G);
-          G = fmaf(w01, __ldg(f01 + kk), G);
-          G = fmaf(w11, __ldg(f11 + kk), G);
-        }
-        lp = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(__ldg(a.wave_z + k), alpha));
-      }
-      const float lp_next = __shfl_down_sync(0xffffffffu, lp, 1);
-      const float G_next = __shfl_down_sync(0xffffffffu, G, 1);
-      float lp_prev = __shfl_up_sync(0xffffffffu, lp, 1);
-      if (lane == 0)
-        lp_prev = (k - 1 >= 0 && k - 1 < nW) ? __fmul_rn(__ldg(a.wave_z + k - 1), alpha) : lp;
-      if (lane < 31 && e < n_e) {
-        float slope = 0.f;
-        if (k >= 0 && k + 1 < nW) {
-          const float dl = lp_next - lp;
-          slope = dl > 0.f ? __fdividef(G_next - G, dl) : 0.f;
-        }
-        const float lpx = lp;
-        const float lpw = (k + 1 >= nW) ? kFltMax : lp_next;
-        row[e] = make_float4(lpx, slope, G, lpw);
-        // T term: G_k * (lambda'_k - lambda'_{k-1}) for lambda'_k inside the telescope range.
-        if (k >= 1 && k < nW && lp >= t_lo && lp <= t_hi) tsum = fmaf(G, lp - lp_prev, tsum);
-      }
+  }
+  mbar_arrive_expect_tx(bar, bytes);
+#pragma unroll
+  for (int p = 0; p < kPB; ++p)
+    if (cells[p] >= 0)
+      bulk_copy_g2s(stage + (size_t)p * a.row_cap, a.ct + (long long)cells[p] * a.n_wave + klo[p],
+                    16u * nk[p], bar);
+}
+
+struct RowParams {
+  float alpha, w00, w10, w01, w11;
+  int ks, klo, khi, n_e;
+  bool has_cell;
+  const float4* st;  // st[k] = staged corners of SSP wavelength k
+  float4* row;
+};
+
+__device__ __forceinline__ RowParams row_params(const ParticleRec& r, int nW,
+                                                const float4* stage, float4* row) {
+  RowParams q;
+  const float tz = r.a.w, ta = __int_as_float(r.b.w);
+  const int ke = r.b.z & ~kGenericFlag;
+  q.alpha = r.a.y;
+  q.w00 = (1.f - tz) * (1.f - ta);
+  q.w10 = tz * (1.f - ta);
+  q.w01 = (1.f - tz) * ta;
+  q.w11 = tz * ta;
+  q.ks = r.b.y;
+  q.klo = max(q.ks, 0);
+  q.khi = min(ke + 1, nW - 1);
+  q.n_e = ke - q.ks + 1;
+  q.has_cell = r.b.x >= 0;
+  q.st = stage - q.klo;
+  q.row = row;
+  return q;
+}
+
+// One warp step of a row build: entries base .. base+30 (lane 31 supplies the right
+// neighbour).  Entry e (SSP index k = kstart + e) = (lambda'_k, slope_k, G_k,
+// lambda'_{k+1}), with sentinels (-FLT_MAX, 0, G_0, lambda'_0) for k = -1 and
+// slope 0 / FLT_MAX beyond the grid.
+__device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
+                                           const float* __restrict__ s_wz, int lane) {
+  const int e = base + lane;
+  const int k = q.ks + e;
+  if (q.ks + base >= 0 && q.ks + base + 31 <= q.khi) {
+    // interior step: every lane, neighbour included, is a staged SSP wavelength
+    float G = 0.f;
+    if (q.has_cell) {
+      const float4 c = q.st[k];
+      G = q.w00 * c.x;
+      G = fmaf(q.w10, c.y, G);
+      G = fmaf(q.w01, c.z, G);
+      G = fmaf(q.w11, c.w, G);
     }
-    tsum = warp_sum(tsum);
-    if (lane == 0) red[warp * kPB + p].x = tsum;
+    const float lp = __fmul_rn(s_wz[k], q.alpha);
+    const float lp_next = __shfl_down_sync(0xffffffffu, lp, 1);
+    const float G_next = __shfl_down_sync(0xffffffffu, G, 1);
+    if (lane < 31) {
+      const float dl = lp_next - lp;
+      const float slope = dl > 0.f ? __fdividef(G_next - G, dl) : 0.f;
+      q.row[e] = make_float4(lp, slope, G, lp_next);
+    }
+  } else {
+    const int kk = min(max(k, q.klo), q.khi);
+    float G = 0.f;
+    if (q.has_cell) {
+      const float4 c = q.st[kk];
+      G = q.w00 * c.x;
+      G = fmaf(q.w10, c.y, G);
+      G = fmaf(q.w01, c.z, G);
+      G = fmaf(q.w11, c.w, G);
+    }
+    const float lp = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(s_wz[k], q.alpha));
+    const float lp_next = __shfl_down_sync(0xffffffffu, lp, 1);
+    const float G_next = __shfl_down_sync(0xffffffffu, G, 1);
+    if (lane < 31 && e < q.n_e) {
+      float slope = 0.f;
+      if (k >= 0 && k + 1 < nW) {
+        const float dl = lp_next - lp;
+        slope = dl > 0.f ? __fdividef(G_next - G, dl) : 0.f;
+      }
+      const float lpw = (k + 1 >= nW) ? kFltMax : lp_next;
+      q.row[e] = make_float4(lp, slope, G, lpw);
+    }
+  }
+}
+
+// Builds the rows of the (one or two) particles of a batch, interleaving their steps.
+__device__ __forceinline__ void build_rows(const MainArgs& a, const ParticleRec* recs, int cnt,
+                                           const float* __restrict__ s_wz,
+                                           const float4* __restrict__ stage,
+                                           float4* __restrict__ rows, int lane, int warp) {
+  const RowParams q0 = row_params(recs[0], a.n_wave, stage, rows);
+  if (cnt > 1) {
+    const RowParams q1 = row_params(recs[1], a.n_wave, stage + a.row_cap, rows + a.row_cap);
+    const int n_max = max(q0.n_e, q1.n_e);
+    for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
+      if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
+      if (base < q1.n_e) build_step(q1, base, a.n_wave, s_wz, lane);
+    }
+  } else {
+    for (int base = warp * 31; base < q0.n_e; base += kAccWarps * 31)
+      build_step(q0, base, a.n_wave, s_wz, lane);
+  }
+}
+
+// Sums 2 values over the 32 lanes with 5 shuffles; lane 0 ends with the total of v0,
+// lane 16 with the total of v1.
+__device__ __forceinline__ float warp_reduce2(float v0, float v1, int lane) {
+  const bool hi = lane & 16;
+  float c = hi ? v1 : v0;
+  c += __shfl_xor_sync(0xffffffffu, hi ? v0 : v1, 16);
+  c += __shfl_xor_sync(0xffffffffu, c, 8);
+  c += __shfl_xor_sync(0xffffffffu, c, 4);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  return c;
+}
+
+// Interpolated values of one particle at this thread's R wavelengths; returns the
+// partial sum of I_t * dlambda_t.
+template <int R, bool kGeneric>
+__device__ __forceinline__ float eval_particle(const float4* __restrict__ rowp, int ks, int ke,
+                                               float B, float A0,
+                                               const int2* __restrict__ s_bucket,
+                                               const float (&lam)[R], const float (&dlam)[R],
+                                               float (&I)[R]) {
+  const float u = A0 - B;
+  int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
+  b = min(max(b, 0), kBuckets - 1);
+  const int2 te = s_bucket[b];
+  int k = te.x + (u >= __int_as_float(te.y) ? 1 : 0);
+  k = min(max(k, ks), ke);
+  float4 e = rowp[k];
+  {
+    const float x = lam[0];
+    while (k > ks && x < e.x) { --k; e = rowp[k]; }
+    while (k < ke && x >= e.w) { ++k; e = rowp[k]; }
+  }
+  float tp = 0.f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float x = lam[r];
+    if (kGeneric) {
+      while (k < ke && x >= e.w) { ++k; e = rowp[k]; }
+    } else if (r > 0 && x >= e.w) {
+      ++k;
+      e = rowp[k];
+    }
+    const float v = fmaf(x - e.x, e.y, e.z);
+    I[r] = v;
+    tp = fmaf(v, dlam[r], tp);
+  }
+  return tp;
+}
+
+// LSF along wavelength of one spectrum: s_pad holds the spectrum at offset
+// lead = K-1-crop with zeros around it, so out[t] = sum_j taps[j] * s_pad[t + K-1 - j].
+template <int R>
+__device__ __forceinline__ void lsf_epilogue(const MainArgs& a, const float* __restrict__ s_pad,
+                                             int t0, float (&out)[R]) {
+#pragma unroll
+  for (int r = 0; r < R; ++r) out[r] = 0.f;
+  const int K = a.lsf_k;
+  const float* base = s_pad + t0 + K - 1;
+  for (int j = 0; j < K; ++j) {
+    const float w = a.lsf[j];
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[r] = fmaf(w, base[r - j], out[r]);
   }
 }
 
 template <int R>
 __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  int2* s_bucket = reinterpret_cast<int2*>(smem);
-  float4* s_rows = reinterpret_cast<float4*>(smem + sizeof(int2) * kBuckets);  // [2][kPB][row_cap]
-  float2* s_red = reinterpret_cast<float2*>(s_rows + 2 * kPB * a.row_cap);       // [3][warps][kPB]
-  float* s_redm = reinterpret_cast<float*>(s_red + 3 * kAccWarps * kPB);         // [3][kPB]
-  BatchMeta* s_meta = reinterpret_cast<BatchMeta*>(s_redm + 4 * kPB);            // [2]
-  __shared__ int s_item, s_last;
+  const SmemLayout SL = smem_layout(a.n_wave, a.row_cap);
+  float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
+  int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
+  float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);
+  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);
+  float* s_red = reinterpret_cast<float*>(smem + SL.red);            // [2][warps][2]
+  ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);  // records of the item
+  float* s_spec = reinterpret_cast<float*>(s_rows);  // LSF epilogue reuses the rows
+  __shared__ uint64_t s_bar;
+  __shared__ int s_item, s_last, s_fail;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < a.n_wave; i += kAccThreads) s_wz[i] = a.wave_z[i];
   for (int b = tid; b < kBuckets; b += kAccThreads) s_bucket[b] = a.bucket[b];
+  if (tid == 0) {
+    mbar_init(&s_bar, 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
 
   const int n_t = a.n_t;
-  float A[R], lam[R], dlam[R], acc[R];
+  const int t0 = tid * R;
+  float lam[R], dlam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    int t = tid + r * kAccThreads;
-    int tc = t < n_t ? t : n_t - 1;
-    A[r] = a.At[tc];
+    const int t = t0 + r;
+    const int tc = t < n_t ? t : n_t - 1;
     lam[r] = a.wave_t[tc];
     dlam[r] = (t < n_t && t > 0) ? (a.wave_t[t] - a.wave_t[t - 1]) : 0.f;
   }
+  const float A0 = a.At[t0 < n_t ? t0 : n_t - 1];
   const int n_items = a.ctrl->n_items;
+  uint32_t phase = 0;
   __syncthreads();
 
   for (;;) {
@@ -321,120 +576,123 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
 
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = 0.f;
-
-    if (nbatch > 0) {
-      build_rows(a, jb, min(kPB, np), s_rows, &s_meta[0], s_red, s_redm, lane, warp);
-      __syncthreads();
+    // records of this item into shared memory (one 48-byte record per thread)
+    for (int i = tid; i < np; i += kAccThreads) {
+      const ParticleRec rr = a.rec[jb + i];
+      s_rec[i] = rr;
     }
+    __syncthreads();
+    if (nbatch > 0 && tid == 0) issue_stage(a, s_rec, min(kPB, np), s_stage, &s_bar);
+
     for (int bt = 0; bt < nbatch; ++bt) {
-      const int buf = bt & 1, slot = bt % 3;
+      const int buf = bt & 1;
       const int cnt = min(kPB, np - bt * kPB);
+      const ParticleRec* recs = s_rec + bt * kPB;
+      if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
+      phase ^= 1u;
+      build_rows(a, recs, cnt, s_wz, s_stage, s_rows, lane, warp);
+      __syncthreads();  // rows ready; staging consumed
+      if (s_fail) {
+        if (tid == 0) {
+          atomicExch(&a.ctrl->error, 1);
+          mbar_wait_bounded(&s_bar, phase ^ 1u);  // give copies in flight a last chance
+        }
+        return;
+      }
+      if (bt + 1 < nbatch && tid == 0)
+        issue_stage(a, recs + kPB, min(kPB, np - (bt + 1) * kPB), s_stage, &s_bar);
       float I[kPB][R];
-      const BatchMeta meta = s_meta[buf];
+      float tp[kPB];
 #pragma unroll
       for (int p = 0; p < kPB; ++p) {
+        tp[p] = 0.f;
         if (p < cnt) {
-          const int ks = meta.ks[p], ke = meta.ke[p];
-          const float B = meta.B[p];
-          const float4* rowp = s_rows + (buf * kPB + p) * a.row_cap - ks;
-          float tp = 0.f;
+          const float B = recs[p].a.z;
+          const int4 rb = recs[p].b;
+          const int ks = rb.y, ke = rb.z & ~kGenericFlag;
+          const float4* rowp = s_rows + p * a.row_cap - ks;
+          tp[p] = (rb.z & kGenericFlag)
+                      ? eval_particle<R, true>(rowp, ks, ke, B, A0, s_bucket, lam, dlam, I[p])
+                      : eval_particle<R, false>(rowp, ks, ke, B, A0, s_bucket, lam, dlam, I[p]);
+        } else {
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const float u = A[r] - B;
-            int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
-            b = min(max(b, 0), kBuckets - 1);
-            const int2 te = s_bucket[b];
-            int k = te.x + (u >= __int_as_float(te.y) ? 1 : 0);
-            k = min(max(k, ks), ke);
-            float4 e = rowp[k];
-            const float x = lam[r];
-            if (x < e.x) {
-              while (k > ks && x < e.x) { --k; e = rowp[k]; }
-            } else if (x >= e.w) {
-              while (k < ke && x >= e.w) { ++k; e = rowp[k]; }
-            }
-            const float v = fmaf(x - e.x, e.y, e.z);
-            I[p][r] = v;
-            tp = fmaf(v, dlam[r], tp);
-          }
-          tp = warp_sum(tp);
-          if (lane == 0) s_red[(slot * kAccWarps + warp) * kPB + p].y = tp;
+          for (int r = 0; r < R; ++r) I[p][r] = 0.f;
         }
       }
-      if (bt + 1 < nbatch) {
-        const int nslot = (bt + 1) % 3;
-        build_rows(a, jb + (long long)(bt + 1) * kPB, min(kPB, np - (bt + 1) * kPB),
-                   s_rows + (buf ^ 1) * kPB * a.row_cap, &s_meta[buf ^ 1],
-                   s_red + nslot * kAccWarps * kPB, s_redm + nslot * kPB, lane, warp);
-      }
+      // T'0, T'1 over the warp, then over the block (fixed order: deterministic).
+      const float wsum = warp_reduce2(tp[0], tp[1], lane);
+      if ((lane & 15) == 0) s_red[(buf * kAccWarps + warp) * 2 + (lane >> 4)] = wsum;
       __syncthreads();
-      float beta[kPB];
-#pragma unroll
-      for (int p = 0; p < kPB; ++p) {
-        beta[p] = 0.f;
-        if (p < cnt) {
-          float T = 0.f, Tn = 0.f;
-#pragma unroll
-          for (int w = 0; w < kAccWarps; ++w) {
-            float2 v = s_red[(slot * kAccWarps + w) * kPB + p];
-            T += v.x;
-            Tn += v.y;
-          }
-          const float m = s_redm[slot * kPB + p];
-          float sc = T / Tn;
-          if (sc != sc) sc = 0.f;
-          if (isinf(sc)) sc = copysignf(kFltMax, sc);
-          beta[p] = (m == 0.f) ? 0.f : m * sc;
-        }
+      float v = (lane < 16) ? s_red[(buf * kAccWarps + (lane & 7)) * 2 + (lane >> 3)] : 0.f;
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      // lane 0: T'0, lane 8: T'1
+      float beta_l = 0.f;
+      if (lane == 0 || lane == 8) {
+        const int p = lane >> 3;
+        const float4 ra = recs[p].a, rc = recs[p].c;  // lane-dependent index: shared memory
+        float sc = rc.x / v;
+        if (sc != sc) sc = 0.f;
+        if (isinf(sc)) sc = copysignf(kFltMax, sc);
+        const float m = ra.x;
+        beta_l = (p < cnt && m != 0.f) ? m * sc : 0.f;
       }
+      const float beta0 = __shfl_sync(0xffffffffu, beta_l, 0);
+      const float beta1 = __shfl_sync(0xffffffffu, beta_l, 8);
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        float add = beta[0] * I[0][r];
-#pragma unroll
-        for (int p = 1; p < kPB; ++p)
-          if (p < cnt) add = fmaf(beta[p], I[p][r], add);
-        acc[r] += add;
-      }
+      for (int r = 0; r < R; ++r) acc[r] += fmaf(beta1, I[1][r], beta0 * I[0][r]);
     }
 
     const int nch = cnt_s <= kChunk ? 1 : (cnt_s + kChunk - 1) / kChunk;
-    if (nch == 1) {
-      float* out = a.cube + (long long)s * a.spaxel_stride;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        int t = tid + r * kAccThreads;
-        if (t < n_t) out[t] = acc[r];
-      }
-    } else {
+    bool have_final = true;
+    if (nch > 1) {
       float* part = a.partials + (long long)item * n_t;
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        int t = tid + r * kAccThreads;
-        if (t < n_t) part[t] = acc[r];
-      }
+      for (int r = 0; r < R; ++r)
+        if (t0 + r < n_t) part[t0 + r] = acc[r];
       __threadfence();
       __syncthreads();
       if (tid == 0) s_last = (atomicAdd(&a.done[s], 1) == nch - 1) ? 1 : 0;
       __syncthreads();
-      if (s_last) {
+      have_final = s_last != 0;
+      if (have_final) {
         __threadfence();
         const long long slot0 = a.slot_start[s];
-        float* out = a.cube + (long long)s * a.spaxel_stride;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          int t = tid + r * kAccThreads;
+          const int t = t0 + r;
+          float sum = 0.f, comp = 0.f;
           if (t < n_t) {
-            float sum = 0.f, comp = 0.f;
             for (int c = 0; c < nch; ++c) {
-              float y = __ldcg(a.partials + (slot0 + c) * n_t + t) - comp;
-              float tt = sum + y;
+              const float y = __ldcg(a.partials + (slot0 + c) * n_t + t) - comp;
+              const float tt = sum + y;
               comp = (tt - sum) - y;
               sum = tt;
             }
-            out[t] = sum;
           }
+          acc[r] = sum;
         }
       }
+    }
+    if (have_final) {
+      float* out = a.cube + (long long)s * a.spaxel_stride;
+      if (a.lsf_k > 0) {
+        __syncthreads();  // rows free (last batch evaluated) before reuse as spectrum
+        const int lead = a.lsf_k - 1 - a.lsf_crop;
+        // zero padding: [0, lead) and [lead + n_t, lead + R*256 + K)
+        for (int i = tid; i < lead; i += kAccThreads) s_spec[i] = 0.f;
+        for (int i = lead + n_t + tid; i < lead + kAccThreads * R + a.lsf_k; i += kAccThreads)
+          s_spec[i] = 0.f;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (t0 + r < n_t) s_spec[lead + t0 + r] = acc[r];
+        __syncthreads();
+        lsf_epilogue<R>(a, s_spec, t0, acc);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (t0 + r < n_t) out[t0 + r] = acc[r];
     }
     __syncthreads();
   }
@@ -444,9 +702,12 @@ struct CubeLayout {
   CubeCtrl* ctrl;
   float* At;
   int2* bucket;
+  float4* ct;
+  double* prefix;
   ParticleRec* rec;
   int* slot_cnt;
-  int* single_cnt;
+  int* big_cnt;
+  int* small_cnt;
   int2* items;
   int* done;
   float* partials;
@@ -455,15 +716,18 @@ struct CubeLayout {
 
 long long max_slots(long long n) { return 2 * ((n + kChunk - 1) / kChunk); }
 
-CubeLayout carve_cube(void* ws, long long n, int n_seg, int n_t) {
+CubeLayout carve_cube(void* ws, long long n, int n_seg, int n_t, int nZ, int nA, int nW) {
   Carve c(ws);
   CubeLayout L;
   L.ctrl = c.take<CubeCtrl>(1);
   L.At = c.take<float>((size_t)n_t);
   L.bucket = c.take<int2>(kBuckets);
+  L.ct = c.take<float4>((size_t)(nZ > 1 ? nZ - 1 : 0) * (nA > 1 ? nA - 1 : 0) * nW);
+  L.prefix = c.take<double>((size_t)nZ * nA * nW);
   L.rec = c.take<ParticleRec>((size_t)(n > 0 ? n : 1));
   L.slot_cnt = c.take<int>((size_t)n_seg + 1);
-  L.single_cnt = c.take<int>((size_t)n_seg + 1);
+  L.big_cnt = c.take<int>((size_t)n_seg + 1);
+  L.small_cnt = c.take<int>((size_t)n_seg + 1);
   L.items = c.take<int2>((size_t)(max_slots(n) + n_seg));
   L.done = c.take<int>((size_t)n_seg);
   L.partials = c.take<float>((size_t)max_slots(n) * n_t);
@@ -485,7 +749,7 @@ int launch_main(const MainArgs& args, size_t smem, cudaStream_t st) {
     return set_error(RUBIX_E_UNSUPPORTED,
                      "cube_main_kernel does not fit on an SM with %zu bytes of shared memory",
                      smem);
-  int grid = sm_count() * per_sm;
+  const int grid = sm_count() * per_sm;
   cube_main_kernel<R><<<grid, kAccThreads, smem, st>>>(args);
   RUBIX_LAUNCH_CHECK("cube_main_kernel");
   return RUBIX_OK;
@@ -497,10 +761,9 @@ int launch_main(const MainArgs& args, size_t smem, cudaStream_t st) {
 using namespace rubix;
 
 extern "C" size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
-                                            int32_t n_wave) {
-  (void)n_wave;
-  if (n < 0 || n_segments < 0 || n_wave_t < 0) return 0;
-  return carve_cube(nullptr, n, n_segments, n_wave_t).bytes;
+                                            int32_t n_met, int32_t n_age, int32_t n_wave) {
+  if (n < 0 || n_segments < 0 || n_wave_t < 0 || n_met < 0 || n_age < 0 || n_wave < 0) return 0;
+  return carve_cube(nullptr, n, n_segments, n_wave_t, n_met, n_age, n_wave).bytes;
 }
 
 extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,
@@ -510,6 +773,7 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
                               const float* age, const float* velocity, int64_t vel_stride,
                               int32_t vel_component, const int32_t* perm,
                               const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                              const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
                               float* cube, int64_t spaxel_stride, void* workspace,
                               size_t workspace_bytes, void* stream) {
   RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "rubix_cube_fwd: bad n");
@@ -523,52 +787,76 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
                 "rubix_cube_fwd: spaxel_stride < n_wave_t");
   RUBIX_REQUIRE(vel_component >= 0 && vel_component < vel_stride, RUBIX_E_INVALID,
                 "rubix_cube_fwd: vel_component outside the velocity row");
+  RUBIX_REQUIRE(n_lsf_taps >= 0 && n_lsf_taps <= kMaxLsfTaps, RUBIX_E_SHAPE,
+                "rubix_cube_fwd: at most %d LSF taps", kMaxLsfTaps);
+  RUBIX_REQUIRE(n_lsf_taps == 0 || (lsf_taps && lsf_crop >= 0 && lsf_crop < n_lsf_taps),
+                RUBIX_E_INVALID, "rubix_cube_fwd: bad LSF taps/crop");
   if (n_segments == 0) return RUBIX_OK;
   RUBIX_REQUIRE(ssp_flux && ssp_metallicity && ssp_age && ssp_wave_z && wave_t && seg_offsets &&
                     cube,
                 RUBIX_E_INVALID, "rubix_cube_fwd: null pointer");
   RUBIX_REQUIRE(n == 0 || (mass && metallicity && age && velocity && perm), RUBIX_E_INVALID,
                 "rubix_cube_fwd: null particle pointer");
-  const size_t need = rubix_cube_workspace_size(n, n_segments, n_wave_t, n_wave);
+  const size_t need = rubix_cube_workspace_size(n, n_segments, n_wave_t, n_met, n_age, n_wave);
   RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
                 "rubix_cube_fwd: workspace of %zu bytes needed, %zu given", need,
                 workspace_bytes);
+  RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
+                "rubix_cube_fwd: workspace must be 256-byte aligned");
   const int row_cap = n_wave + 2;
-  const size_t smem = sizeof(int2) * kBuckets + sizeof(float4) * 2 * kPB * row_cap +
-                      sizeof(float2) * 3 * kAccWarps * kPB + sizeof(float) * 4 * kPB +
-                      sizeof(BatchMeta) * 2;
-  RUBIX_REQUIRE(smem <= 227 * 1024, RUBIX_E_UNSUPPORTED,
-                "rubix_cube_fwd: SSP grid of %d wavelengths needs %zu bytes of shared memory",
-                n_wave, smem);
+  const SmemLayout SL = smem_layout(n_wave, row_cap);
+  // Up to about 1300 SSP wavelengths two blocks fit on an SM; larger grids run one.
+  RUBIX_REQUIRE(SL.total <= 227 * 1024, RUBIX_E_UNSUPPORTED,
+                "rubix_cube_fwd: SSP grid of %d wavelengths needs %zu bytes of shared memory "
+                "(limit 232448)",
+                n_wave, SL.total);
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  CubeLayout L = carve_cube(workspace, n, n_segments, n_wave_t);
-  cube_setup_kernel<<<1, 256, 0, st>>>(ssp_wave_z, n_wave, wave_t, n_wave_t, L.ctrl, L.At,
-                                       L.bucket);
-  RUBIX_LAUNCH_CHECK("cube_setup_kernel");
+  CubeLayout L = carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave);
+  RUBIX_CUDA_TRY(cudaMemsetAsync(&L.ctrl->dz_min_bits, 0xff, sizeof(unsigned), st));
+  RUBIX_CUDA_TRY(cudaMemsetAsync(&L.ctrl->dt_max_bits, 0, sizeof(unsigned), st));
+  {
+    const int work = std::max(std::max(n_wave_t, n_wave), kBuckets);
+    cube_setup_kernel<<<div_up(work, 128), 128, 0, st>>>(ssp_wave_z, n_wave, wave_t, n_wave_t,
+                                                         L.ctrl, L.At, L.bucket);
+    RUBIX_LAUNCH_CHECK("cube_setup_kernel");
+  }
+  {
+    const long long total = (long long)(n_met - 1) * (n_age - 1) * n_wave;
+    const int g = (int)std::min<long long>((total + 255) / 256, (long long)sm_count() * 8);
+    cube_corner_table_kernel<<<g, 256, 0, st>>>(ssp_flux, n_met, n_age, n_wave, L.ct);
+    RUBIX_LAUNCH_CHECK("cube_corner_table_kernel");
+    const int rows = n_met * n_age;
+    cube_prefix_kernel<<<div_up(rows, 64), 64, 0, st>>>(ssp_flux, rows, n_wave, ssp_wave_z,
+                                                         L.prefix);
+    RUBIX_LAUNCH_CHECK("cube_prefix_kernel");
+  }
   if (n > 0) {
-    int g = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
+    const int g = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
     cube_gather_kernel<<<g, 256, 0, st>>>(mass, metallicity, age, velocity, vel_stride,
                                           vel_component, perm, seg_offsets, n_segments, n,
                                           ssp_metallicity, n_met, ssp_age, n_age, ssp_wave_z,
-                                          n_wave, wave_t, n_wave_t, L.ctrl, L.rec);
+                                          n_wave, wave_t, n_wave_t, L.prefix, L.ctrl, L.rec);
     RUBIX_LAUNCH_CHECK("cube_gather_kernel");
   }
   {
-    int g = (int)std::min<long long>((n_segments + 255) / 256, (long long)sm_count() * 8);
-    cube_count_kernel<<<g, 256, 0, st>>>(seg_offsets, n_segments, L.slot_cnt, L.single_cnt);
+    const int g = (int)std::min<long long>((n_segments + 255) / 256, (long long)sm_count() * 8);
+    cube_count_kernel<<<g, 256, 0, st>>>(seg_offsets, n_segments, L.slot_cnt, L.big_cnt,
+                                         L.small_cnt);
     RUBIX_LAUNCH_CHECK("cube_count_kernel");
     scan_exclusive_1block<<<1, 1024, 0, st>>>(L.slot_cnt, n_segments, 1);
     RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
-    scan_exclusive_1block<<<1, 1024, 0, st>>>(L.single_cnt, n_segments, 1);
+    scan_exclusive_1block<<<1, 1024, 0, st>>>(L.big_cnt, n_segments, 1);
     RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
-    cube_fill_items_kernel<<<g, 256, 0, st>>>(seg_offsets, n_segments, L.slot_cnt, L.single_cnt,
-                                              L.items, L.ctrl);
+    scan_exclusive_1block<<<1, 1024, 0, st>>>(L.small_cnt, n_segments, 1);
+    RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
+    cube_fill_items_kernel<<<g, 256, 0, st>>>(seg_offsets, n_segments, L.slot_cnt, L.big_cnt,
+                                              L.small_cnt, L.items, L.ctrl);
     RUBIX_LAUNCH_CHECK("cube_fill_items_kernel");
     RUBIX_CUDA_TRY(cudaMemsetAsync(L.done, 0, sizeof(int) * (size_t)n_segments, st));
   }
   MainArgs args;
-  args.flux = ssp_flux;
+  args.ct = L.ct;
   args.wave_z = ssp_wave_z;
   args.nZ = n_met;
   args.nA = n_age;
@@ -587,10 +875,28 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
   args.ctrl = L.ctrl;
   args.bucket = L.bucket;
   args.row_cap = row_cap;
-  const int R = (n_wave_t + kAccThreads - 1) / kAccThreads;
-  if (R <= 1) return launch_main<1>(args, smem, st);
-  if (R <= 2) return launch_main<2>(args, smem, st);
-  if (R <= 4) return launch_main<4>(args, smem, st);
-  if (R <= 8) return launch_main<8>(args, smem, st);
+  args.lsf_k = n_lsf_taps;
+  args.lsf_crop = lsf_crop;
+  for (int i = 0; i <= kMaxLsfTaps; ++i) args.lsf[i] = i < n_lsf_taps ? lsf_taps[i] : 0.f;
+  const int need_r = (n_wave_t + kAccThreads - 1) / kAccThreads;
+  const size_t smem = SL.total;
+  if (need_r <= 1) return launch_main<1>(args, smem, st);
+  if (need_r <= 2) return launch_main<2>(args, smem, st);
+  if (need_r <= 4) return launch_main<4>(args, smem, st);
+  if (need_r <= 8) return launch_main<8>(args, smem, st);
+  if (need_r <= 12) return launch_main<12>(args, smem, st);
+  if (need_r <= 15) return launch_main<15>(args, smem, st);
   return launch_main<16>(args, smem, st);
+}
+
+extern "C" int rubix_cube_status(const void* workspace, int* device_error, void* stream) {
+  RUBIX_REQUIRE(workspace != nullptr && device_error != nullptr, RUBIX_E_INVALID,
+                "rubix_cube_status: null pointer");
+  const CubeCtrl* ctrl = static_cast<const CubeCtrl*>(workspace);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  RUBIX_CUDA_TRY(cudaMemcpyAsync(device_error, &ctrl->error, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+  RUBIX_CUDA_TRY(cudaStreamSynchronize(st));
+  return *device_error ? set_error(RUBIX_E_DEVICE, "cube kernel: a TMA wait timed out")
+                       : RUBIX_OK;
 }

@@ -88,6 +88,106 @@ __global__ void __launch_bounds__(kPsfThreads) psf_strip_kernel(PsfArgs a) {
   }
 }
 
+
+// Register-blocked variant for equal odd-or-even tap counts M <= 25: each thread owns
+// one wavelength lane and kPsfXB consecutive x positions; the y window of the last M
+// x-convolved rows lives in registers (the row loop is unrolled by M so every window
+// index is static) and the next input row is prefetched into registers while the
+// current one is convolved, so each row costs one barrier.
+constexpr int kPsfXB = 4;
+
+template <int M>
+__global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
+  constexpr int W = kPsfTileX + M - 1;  // staged row width
+  constexpr int PER = (W * kPsfTileL + kPsfThreads - 1) / kPsfThreads;
+  __shared__ float s_in[2][W * kPsfTileL];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int x0 = blockIdx.x * kPsfTileX;
+  const int l0 = blockIdx.y * kPsfTileL;
+  const int l = l0 + lane;
+  const int xsrc0 = x0 - (M - 1) + a.ox;
+  const int xb = warp * kPsfXB;  // first local x of this thread
+  float ty[M], tx[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    ty[i] = a.ty[i];
+    tx[i] = a.tx[i];
+  }
+  const int total = a.ny + a.oy;  // input rows 0 .. ny-1+oy
+  float pre[PER];
+  auto load_row = [&](int r) {
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int q = tid + k * kPsfThreads;
+      float v = 0.f;
+      if (q < W * kPsfTileL && r < a.ny) {
+        const int jj = q / kPsfTileL, ll = q % kPsfTileL;
+        const int xg = xsrc0 + jj, lg = l0 + ll;
+        if (xg >= 0 && xg < a.nx && lg < a.nl) v = a.in[((long long)r * a.nx + xg) * a.sin + lg];
+      }
+      pre[k] = v;
+    }
+  };
+  auto store_row = [&](int buf) {
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int q = tid + k * kPsfThreads;
+      if (q < W * kPsfTileL) s_in[buf][q] = pre[k];
+    }
+  };
+  float win[M][kPsfXB];
+#pragma unroll
+  for (int i = 0; i < M; ++i)
+#pragma unroll
+    for (int j = 0; j < kPsfXB; ++j) win[i][j] = 0.f;
+
+  load_row(0);
+  store_row(0);
+  __syncthreads();
+  for (int r0 = 0; r0 < total; r0 += M) {
+#pragma unroll
+    for (int jj = 0; jj < M; ++jj) {
+      const int r = r0 + jj;
+      if (r >= total) break;
+      const int buf = r & 1;
+      if (r + 1 < total) load_row(r + 1);
+      // x-pass over the staged row r for this thread's kPsfXB positions
+      float xv[kPsfXB + M - 1];
+#pragma unroll
+      for (int q = 0; q < kPsfXB + M - 1; ++q) xv[q] = s_in[buf][(xb + q) * kPsfTileL + lane];
+#pragma unroll
+      for (int j = 0; j < kPsfXB; ++j) {
+        float h = 0.f;
+#pragma unroll
+        for (int i = 0; i < M; ++i) h = fmaf(tx[i], xv[j + (M - 1) - i], h);
+        win[jj][j] = h;
+      }
+      // y-pass: output row y = r - oy uses x-convolved rows r - i, i < M
+      const int y = r - a.oy;
+      if (y >= 0 && l < a.nl) {
+#pragma unroll
+        for (int j = 0; j < kPsfXB; ++j) {
+          float o = 0.f;
+#pragma unroll
+          for (int i = 0; i < M; ++i) o = fmaf(ty[i], win[(jj - i + M) % M][j], o);
+          const int x = x0 + xb + j;
+          if (x < a.nx) a.out[((long long)y * a.nx + x) * a.sout + l] = o;
+        }
+      }
+      if (r + 1 < total) store_row(buf ^ 1);
+      __syncthreads();
+    }
+  }
+}
+
+template <int M>
+int launch_psf_reg(const PsfArgs& a, cudaStream_t st) {
+  dim3 grid(div_up(a.nx, kPsfTileX), div_up(a.nl, kPsfTileL));
+  psf_reg_kernel<M><<<grid, kPsfThreads, 0, st>>>(a);
+  RUBIX_LAUNCH_CHECK("psf_reg_kernel");
+  return RUBIX_OK;
+}
+
 }  // namespace
 }  // namespace rubix
 
@@ -122,6 +222,23 @@ extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx
     a.ty[i] = i < m_y ? ty[i] : 0.f;
     a.tx[i] = i < m_x ? tx[i] : 0.f;
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (m_x == m_y) {
+    switch (m_x) {
+      case 1: return launch_psf_reg<1>(a, st);
+      case 3: return launch_psf_reg<3>(a, st);
+      case 5: return launch_psf_reg<5>(a, st);
+      case 7: return launch_psf_reg<7>(a, st);
+      case 9: return launch_psf_reg<9>(a, st);
+      case 11: return launch_psf_reg<11>(a, st);
+      case 13: return launch_psf_reg<13>(a, st);
+      case 15: return launch_psf_reg<15>(a, st);
+      case 17: return launch_psf_reg<17>(a, st);
+      case 19: return launch_psf_reg<19>(a, st);
+      case 21: return launch_psf_reg<21>(a, st);
+      default: break;
+    }
+  }
   const size_t smem = sizeof(float) * ((size_t)(kPsfTileX + m_x - 1) * kPsfTileL +
                                        (size_t)m_y * kPsfTileX * kPsfTileL);
   cudaError_t e = cudaFuncSetAttribute(psf_strip_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -129,7 +246,7 @@ extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx
   if (e != cudaSuccess)
     return set_error(RUBIX_E_CUDA, "cudaFuncSetAttribute(psf_strip_kernel): %s", cudaGetErrorString(e));
   dim3 grid(div_up(nx, kPsfTileX), div_up(n_wave_t, kPsfTileL));
-  psf_strip_kernel<<<grid, kPsfThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+  psf_strip_kernel<<<grid, kPsfThreads, smem, st>>>(a);
   RUBIX_LAUNCH_CHECK("psf_strip_kernel");
   return RUBIX_OK;
 }

@@ -6,32 +6,48 @@
 namespace rubix {
 namespace {
 
-// Exclusive scan of `count` ints in place by one block of 1024 threads; the grand
-// total is written to data[count] when `with_total` is set (data has count+1 slots).
+// Exclusive scan of `count` ints in place by one block of 1024 threads, in tiles of
+// 4096 (4 consecutive values per thread, warp-shuffle scans).  The grand total is
+// written to data[count] when `with_total` is set (data then has count+1 slots).
 __global__ void __launch_bounds__(1024)
 scan_exclusive_1block(int* __restrict__ data, long long count, int with_total) {
-  __shared__ long long s_part[1024];
-  const int t = threadIdx.x;
-  const long long per = (count + 1023) / 1024;
-  const long long b = t * per;
-  const long long e = b + per < count ? b + per : count;
-  long long sum = 0;
-  for (long long i = b; i < e; ++i) sum += data[i];
-  s_part[t] = sum;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    long long v = (t >= off) ? s_part[t - off] : 0;
+  __shared__ int s_warp[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  long long carry = 0;
+  for (long long base = 0; base < count; base += 4096) {
+    const long long i0 = base + 4LL * t;
+    int v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = (i0 + j < count) ? data[i0 + j] : 0;
+    const int tsum = v[0] + v[1] + v[2] + v[3];
+    int x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
     __syncthreads();
-    s_part[t] += v;
+    if (w == 0) {
+      int ws = s_warp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, ws, o);
+        if (lane >= o) ws += y;
+      }
+      s_warp[lane] = ws;
+    }
+    __syncthreads();
+    long long run = carry + (x - tsum) + (w > 0 ? s_warp[w - 1] : 0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (i0 + j < count) data[i0 + j] = (int)run;
+      run += v[j];
+    }
+    carry += s_warp[31];
     __syncthreads();
   }
-  long long run = (t == 0) ? 0 : s_part[t - 1];
-  for (long long i = b; i < e; ++i) {
-    int v = data[i];
-    data[i] = (int)run;
-    run += v;
-  }
-  if (with_total && t == 1023) data[count] = (int)s_part[1023];
+  if (with_total && t == 0) data[count] = (int)carry;
 }
 
 }  // namespace

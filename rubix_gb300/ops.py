@@ -25,6 +25,19 @@ __all__ = [
 ]
 
 
+# Number of this library's kernels launched through these wrappers (per process).
+LAUNCHES = {"count": 0}
+
+
+def _count(k: int) -> None:
+    LAUNCHES["count"] += int(k)
+
+
+def _sort_passes(n_segments: int) -> int:
+    bits = max(1, int(n_segments).bit_length())
+    return (bits + 7) // 8
+
+
 def _stream(dev: torch.device) -> int:
     return torch.cuda.current_stream(dev).cuda_stream
 
@@ -63,6 +76,7 @@ def aperture_mask(coords: torch.Tensor, edges: torch.Tensor) -> torch.Tensor:
     stride = coords.shape[1] if coords.dim() == 2 else 1
     _lib.call("rubix_aperture_mask", _ptr(coords), n, stride, _ptr(edges), edges.numel(),
               _ptr(out), _stream(coords.device))
+    _count(1 if n > 0 else 0)
     return out
 
 
@@ -76,6 +90,7 @@ def spaxel_assign(coords: torch.Tensor, edges: torch.Tensor) -> torch.Tensor:
     out = torch.empty(n, dtype=torch.int32, device=coords.device)
     _lib.call("rubix_spaxel_assign", _ptr(coords), n, coords.shape[1], _ptr(edges),
               edges.numel(), _ptr(out), _stream(coords.device))
+    _count(1 if n > 0 else 0)
     return out
 
 
@@ -94,12 +109,18 @@ def spaxel_sort(idx: torch.Tensor, n_segments: int, keep: torch.Tensor | None = 
     ws = workspace(nbytes, dev)
     _lib.call("rubix_spaxel_sort", _ptr(idx), _ptr(keep), n, int(n_segments), _ptr(perm),
               _ptr(offs), _ptr(ws), ws.numel(), _stream(dev))
+    _count(2 + 3 * _sort_passes(n_segments) if n > 0 else 0)
     return perm, offs
 
 
 def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, metallicity,
-                 age, velocity, vel_component, perm, seg_offsets, n_segments, out=None):
-    """Fused lookup + mass + Doppler/resample + per-spaxel sum -> cube [n_segments, L]."""
+                 age, velocity, vel_component, perm, seg_offsets, n_segments, out=None,
+                 lsf_taps=None, lsf_crop=0, check=False):
+    """Fused lookup + mass + Doppler/resample + per-spaxel sum -> cube [n_segments, L].
+
+    ``lsf_taps`` (optional) adds the LSF convolution along wavelength of every finished
+    spectrum.  ``check=True`` synchronises the stream and raises if the kernel reported
+    a device error (a timed-out shared-memory copy wait)."""
     ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
     if ssp_flux.dim() != 3:
         raise ValueError("ssp_flux must be [n_met, n_age, n_wave]")
@@ -128,13 +149,21 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
         _check_cuda("out", out, torch.float32)
         if out.dim() != 2 or out.shape[0] != n_segments or out.shape[1] < L or out.stride(1) != 1:
             raise ValueError("out must be [n_segments, >=L] with unit stride along wavelength")
-    nbytes = _lib.query("rubix_cube_workspace_size", n, int(n_segments), L, nw)
+    lsf = None if lsf_taps is None else _host_taps(lsf_taps)
+    nbytes = _lib.query("rubix_cube_workspace_size", n, int(n_segments), L, nz, na, nw)
     ws = workspace(nbytes, dev)
     _lib.call("rubix_cube_fwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
               _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
               _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
-              _ptr(seg_offsets), int(n_segments), n, _ptr(out), out.stride(0), _ptr(ws),
-              ws.numel(), _stream(dev))
+              _ptr(seg_offsets), int(n_segments), n,
+              None if lsf is None else lsf.ctypes.data, 0 if lsf is None else lsf.size,
+              int(lsf_crop), _ptr(out), out.stride(0), _ptr(ws), ws.numel(), _stream(dev))
+    _count((8 + (1 if n > 0 else 0)) if n_segments > 0 else 0)
+    if check and n_segments > 0:
+        import ctypes
+
+        err = ctypes.c_int(0)
+        _lib.call("rubix_cube_status", _ptr(ws), ctypes.byref(err), _stream(dev))
     return out
 
 
@@ -155,6 +184,7 @@ def psf_forward(cube: torch.Tensor, taps_y, taps_x=None, out=None) -> torch.Tens
         out = torch.empty((ny, nx, L), dtype=torch.float32, device=cube.device)
     _lib.call("rubix_psf_fwd", _ptr(cube), _ptr(out), ny, nx, L, cube.stride(1), out.stride(1),
               ty.ctypes.data, ty.size, tx.ctypes.data, tx.size, _stream(cube.device))
+    _count(1 if cube.numel() > 0 else 0)
     return out
 
 
@@ -171,4 +201,5 @@ def lsf_forward(cube: torch.Tensor, taps, crop: int, out=None) -> torch.Tensor:
     orow = out.view(-1, L)
     _lib.call("rubix_lsf_fwd", _ptr(rows), _ptr(orow), rows.shape[0], L, rows.stride(0),
               orow.stride(0), k.ctypes.data, k.size, int(crop), _stream(cube.device))
+    _count(1 if cube.numel() > 0 else 0)
     return out

@@ -76,7 +76,7 @@ def _cube_small(ops, w, keep=True):
     cube = ops.cube_forward(
         to_dev(w.ssp.flux), to_dev(w.ssp.metallicity), to_dev(w.ssp.age), to_dev(w.wave_z),
         to_dev(w.wave_t), to_dev(p.mass), to_dev(p.metallicity), to_dev(p.age),
-        to_dev(p.velocity), 2, perm, offs, nseg,
+        to_dev(p.velocity), 2, perm, offs, nseg, check=True,
     )
     torch.cuda.synchronize()
     return cube.reshape(w.sbin, w.sbin, -1)
@@ -136,3 +136,86 @@ def test_full_chain_small(ops):
     c3 = ops.lsf_forward(c2, tel.lsf_taps(w.lsf_sigma, w.wave_res), 12)
     torch.cuda.synchronize()
     assert_cube_close(c3.cpu().numpy(), ref["final"], what="final cube")
+
+
+def _cube_for(ops, w):
+    import torch
+
+    p = w.particles
+    c = to_dev(p.coords)
+    e = to_dev(w.edges)
+    nseg = w.sbin * w.sbin
+    perm, offs = ops.spaxel_sort(ops.spaxel_assign(c, e), nseg, ops.aperture_mask(c, e))
+    cube = ops.cube_forward(
+        to_dev(w.ssp.flux), to_dev(w.ssp.metallicity), to_dev(w.ssp.age), to_dev(w.wave_z),
+        to_dev(w.wave_t), to_dev(p.mass), to_dev(p.metallicity), to_dev(p.age),
+        to_dev(p.velocity), 2, perm, offs, nseg, check=True)
+    torch.cuda.synchronize()
+    return cube.reshape(w.sbin, w.sbin, -1).cpu().numpy(), offs.cpu().numpy()
+
+
+def test_cube_general_walk_fine_ssp_grid(ops):
+    """SSP grid finer than the telescope bins (the walk may cross several SSP nodes per
+    bin) plus particles beyond +-10^4 km/s."""
+    import dataclasses
+
+    from rubix_gb300 import synth
+
+    base = workload("small", n=3000)
+    rng = np.random.default_rng(7)
+    wave = np.linspace(4000.0, 5400.0, 1400).astype(np.float32)
+    ssp = synth.make_ssp(12, 5, 1400, seed=9)
+    ssp = dataclasses.replace(ssp, wavelength=wave)
+    p = base.particles
+    vel = p.velocity.copy()
+    vel[:40, 2] = rng.uniform(-30000, 30000, 40).astype(np.float32)
+    p2 = dataclasses.replace(p, velocity=vel)
+    wave_t = np.arange(4700.15, 5300.0, 1.25, dtype=np.float32)
+    w = dataclasses.replace(base, particles=p2, ssp=ssp, wave_t=wave_t,
+                            wave_z=oracle.cosmological_doppler_shift(base.dist_z, wave))
+    got, _ = _cube_for(ops, w)
+    ref = oracle.render_cube(p2.coords, p2.velocity, p2.mass, p2.metallicity, p2.age, w.edges,
+                             w.sbin, ssp.metallicity, ssp.age, ssp.flux, wave, w.dist_z, wave_t)
+    assert_cube_close(got, ref["cube"], what="general-walk cube")
+
+
+def test_cube_ifu_sampled_spaxels(ops):
+    """Full 10^6-particle IFU workload; the oracle recomputes a sample of spaxels
+    (including the densest ones, which are split into several chunks and merged)."""
+    w = workload("ifu", edge_cases=False)
+    p = w.particles
+    got, offs = _cube_for(ops, w)
+    counts = np.diff(offs)
+    dense = np.argsort(counts)[-3:]
+    rng = np.random.default_rng(3)
+    occupied = np.nonzero(counts)[0]
+    sample = np.unique(np.concatenate([dense, rng.choice(occupied, 5, replace=False)]))
+    assert counts[dense].max() > 512, "workload should contain multi-chunk spaxels"
+    idx = oracle.square_spaxel_assignment(p.coords, w.edges)
+    inside = oracle.mask_particles_outside_aperture(p.coords, w.edges)
+    for s in sample:
+        sel = np.nonzero((idx == s) & inside)[0]
+        spec = oracle.particle_spectra(p.mass[sel], p.metallicity[sel], p.age[sel],
+                                       p.velocity[sel, 2], w.ssp.metallicity, w.ssp.age,
+                                       w.ssp.flux, w.wave_z, w.wave_t).sum(axis=0)
+        iy, ix = divmod(int(s), w.sbin)
+        assert_cube_close(got[iy, ix], spec, what=f"spaxel {s} ({sel.size} particles)")
+
+
+def test_renderer_fused_lsf_matches_oracle(ops):
+    """Accumulate with the LSF epilogue, then PSF (the renderer's default order)."""
+    import torch
+
+    from rubix_gb300.api import IFURenderer
+
+    w = workload("small")
+    ref = oracle_stages("small")
+    p = w.particles
+    r = IFURenderer.from_workload(w, device="cuda")
+    st = r.render(*(to_dev(a) for a in (p.coords, p.velocity, p.mass, p.metallicity, p.age)))
+    torch.cuda.synchronize()
+    assert st.lsf_fused
+    assert_cube_close(st.final.cpu().numpy(), ref["final"], what="fused final cube")
+    st2 = r.render(*(to_dev(a) for a in (p.coords, p.velocity, p.mass, p.metallicity, p.age)),
+                   fuse_lsf=False)
+    assert_cube_close(st2.final.cpu().numpy(), ref["final"], what="unfused final cube")
