@@ -142,6 +142,32 @@ RUBIX_API int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity
  */
 RUBIX_API int rubix_cube_status(const void* workspace, int* device_error, void* stream);
 
+/*
+ * No counterpart in rubix (rubix has no C interface; JAX allocates its buffers).
+ *
+ * rubix_cube_fwd without the workspace argument, for callers that cannot allocate
+ * device memory when they render: hosts that own all GPU memory through their own
+ * pool and forbid cudaMalloc from plugins, or loops that must never enter an
+ * allocator.  Same inputs, output and results as rubix_cube_fwd; the scratch is a
+ * static device array of RUBIX_CUBE_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * this part of the library keeps until process exit.  Problems needing more scratch
+ * (rubix_cube_workspace_size) return RUBIX_E_WORKSPACE.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps race.
+ */
+#define RUBIX_CUBE_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+RUBIX_API int rubix_cube_fwd_noalloc(const float* ssp_flux, const float* ssp_metallicity,
+                                     const float* ssp_age, const float* ssp_wave_z,
+                                     int32_t n_met, int32_t n_age, int32_t n_wave,
+                                     const float* wave_t, int32_t n_wave_t, const float* mass,
+                                     const float* metallicity, const float* age,
+                                     const float* velocity, int64_t vel_stride,
+                                     int32_t vel_component, const int32_t* perm,
+                                     const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                     const float* lsf_taps, int32_t n_lsf_taps,
+                                     int32_t lsf_crop, float* cube, int64_t spaxel_stride,
+                                     void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* (c) PSF: per-wavelength 2-D convolution, separable Gaussian               */
 /* ------------------------------------------------------------------------- */
