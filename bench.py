@@ -241,10 +241,13 @@ def main():
     torch.cuda.set_device(dev)
 
     from rubix_gb300 import _build, ops, synth
+    from rubix_gb300 import dist as rdist
     from rubix_gb300.api import IFURenderer
 
     _build.build()
-    w = synth.make_workload(args.workload, n=args.particles, edge_cases=False)
+    # every rank renders its own galaxy (independent seeds): weak scaling, no exchange
+    w = synth.make_workload(args.workload, n=args.particles, edge_cases=False,
+                            seed=rdist.rank_seed(synth.WORKLOADS[args.workload]["seed"], rank))
     p = w.particles
     N, L = p.n, int(w.wave_t.size)
     S2 = w.sbin * w.sbin
@@ -293,11 +296,7 @@ def main():
     clocks = sampler.stop()
     launches = ops.LAUNCHES["count"] - n_launch0
 
-    total_ms = sum(step_ms)
-    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = rdist.max_over_ranks(sum(step_ms))
     value = world * N * L * args.steps / (total_ms * 1e-3)
 
     # ---------------- e2e through the public renderer from pinned host buffers
@@ -325,10 +324,8 @@ def main():
             e1.record()
             torch.cuda.synchronize()
             e2e_ms.append(e0.elapsed_time(e1))
-        te = torch.tensor([sum(e2e_ms)], dtype=torch.float64, device=dev)
-        if world > 1:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * N * L * args.steps / (float(te.item()) * 1e-3),
+        te_ms = rdist.max_over_ranks(sum(e2e_ms))
+        e2e = {"value": world * N * L * args.steps / (te_ms * 1e-3),
                "unit": "particle*lambda/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)}
 

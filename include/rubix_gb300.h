@@ -169,6 +169,58 @@ RUBIX_API int rubix_cube_fwd_noalloc(const float* ssp_flux, const float* ssp_met
                                      void* stream);
 
 /* ------------------------------------------------------------------------- */
+/* Materialised intermediates (step-by-step use; the fused path never needs them) */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * out[i][k] = interp2d_linear(metallicity_i, age_i) of ssp_flux[:, :, k], times
+ * mass_i when mass != NULL; 0 outside the grid.  Replaces the lookup of
+ * calculate_spectra (rubix/core/ifu.py:63-121; spectra/ssp/grid.py:113-120 with
+ * method="linear") and, with mass, scale_spectrum_by_mass (core/ifu.py:149-157).
+ */
+RUBIX_API int rubix_ssp_lookup(const float* ssp_flux, const float* ssp_metallicity,
+                               const float* ssp_age, int32_t n_met, int32_t n_age,
+                               int32_t n_wave, const float* metallicity, const float* age,
+                               const float* mass, int64_t n, float* out, int64_t out_stride,
+                               void* stream);
+
+/*
+ * values[i][0..width) = 0 for every i with mask[i] == 0, in place (rows of `stride`
+ * floats): the zeroing of particle fields outside the aperture done by
+ * filter_particles, rubix/core/telescope.py:159-172.
+ */
+RUBIX_API int rubix_mask_zero(float* values, int64_t n, int32_t width, int64_t stride,
+                              const uint8_t* mask, void* stream);
+
+/* out[i][k] = rows[i][k] * mass[i]: scale_spectrum_by_mass, rubix/core/ifu.py:149-157. */
+RUBIX_API int rubix_scale_rows(const float* rows, int64_t row_stride, const float* mass,
+                               int64_t n, int32_t n_wave, float* out, int64_t out_stride,
+                               void* stream);
+
+/*
+ * resample_spectrum (rubix/spectra/ifu.py:224-266) of each given spectrum row i on the
+ * Doppler-shifted grid fl32(ssp_wave_z * fl32(exp(v_i/c))) onto wave_t: the
+ * doppler_shift_and_resampling step (rubix/core/ifu.py:226-295) for spectra the caller
+ * holds.  n_wave <= ~25000.
+ */
+RUBIX_API int rubix_resample_rows(const float* spectra, int64_t spectra_stride,
+                                  const float* ssp_wave_z, int32_t n_wave,
+                                  const float* velocity, int64_t vel_stride,
+                                  int32_t vel_component, int64_t n, const float* wave_t,
+                                  int32_t n_wave_t, float* out, int64_t out_stride,
+                                  void* stream);
+
+/*
+ * out[s] = sum of rows[perm[j]] for j in [seg_offsets[s], seg_offsets[s+1]) in that
+ * order: calculate_cube (rubix/spectra/ifu.py:270-288) for spectra the caller holds,
+ * with (perm, seg_offsets) from rubix_spaxel_sort.
+ */
+RUBIX_API int rubix_segment_sum_rows(const float* rows, int64_t row_stride, int32_t n_wave_t,
+                                     const int32_t* perm, const int32_t* seg_offsets,
+                                     int32_t n_segments, float* out, int64_t out_stride,
+                                     void* stream);
+
+/* ------------------------------------------------------------------------- */
 /* (c) PSF: per-wavelength 2-D convolution, separable Gaussian               */
 /* ------------------------------------------------------------------------- */
 

@@ -332,11 +332,10 @@ def apply_psf(datacube, psf_kernel, method="auto"):
             for j in range(n):
                 # out[y, x] += K[i, j] * in[y + o0 - i, x + o1 - j]
                 dy, dx = o0 - i, o1 - j
-                ys = slice(max(0, -dy), min(S0, S0 - dy))
-                xs = slice(max(0, -dx), min(S1, S1 - dx))
-                yi = slice(ys.start + dy, ys.stop + dy)
-                xi = slice(xs.start + dx, xs.stop + dx)
-                out[ys, xs, :] += K[i, j] * cube[yi, xi, :]
+                y0, y1 = max(0, -dy), min(S0, S0 - dy)
+                x0, x1 = max(0, -dx), min(S1, S1 - dx)
+                if y1 > y0 and x1 > x0:
+                    out[y0:y1, x0:x1, :] += K[i, j] * cube[y0 + dy:y1 + dy, x0 + dx:x1 + dx, :]
         return out
     return _fft_conv_same_2d(cube, K)
 
@@ -366,8 +365,9 @@ def apply_lsf(datacube, lsf_sigma, wave_resolution, extend_factor=12):
     # out[t] = full[t + f] = sum_j g[j] * in[t + f - j]
     for j in range(K):
         d = extend_factor - j
-        ts = slice(max(0, -d), min(L, L - d))
-        out[:, ts] += g[j] * flat[:, ts.start + d : ts.stop + d]
+        lo, hi = max(0, -d), min(L, L - d)
+        if hi > lo:
+            out[:, lo:hi] += g[j] * flat[:, lo + d : hi + d]
     return out.reshape(cube.shape)
 
 

@@ -9,4 +9,9 @@ compute path.  ``rubix_gb300.core`` mirrors rubix's pipeline-step API
 
 __version__ = "0.1.0"
 
-from ._build import build  # noqa: E402,F401
+
+def build(force: bool = False) -> str:
+    """Compile the CUDA library in-tree if it is missing or stale; returns its path."""
+    from ._build import build as _b
+
+    return _b(force=force)

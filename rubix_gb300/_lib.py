@@ -46,6 +46,19 @@ SIGNATURES = {
          _vp, _vp, _vp, _vp, _i64, _i32,
          _vp, _vp, _i32, _i64, _vp, _i32, _i32, _vp, _i64, _vp, _sz, _vp],
     ),
+    "rubix_cube_fwd_noalloc": (
+        _c.c_int,
+        [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32,
+         _vp, _vp, _vp, _vp, _i64, _i32,
+         _vp, _vp, _i32, _i64, _vp, _i32, _i32, _vp, _i64, _vp],
+    ),
+    "rubix_ssp_lookup": (_c.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "rubix_mask_zero": (_c.c_int, [_vp, _i64, _i32, _i64, _vp, _vp]),
+    "rubix_scale_rows": (_c.c_int, [_vp, _i64, _vp, _i64, _i32, _vp, _i64, _vp]),
+    "rubix_resample_rows": (
+        _c.c_int, [_vp, _i64, _vp, _i32, _vp, _i64, _i32, _i64, _vp, _i32, _vp, _i64, _vp]
+    ),
+    "rubix_segment_sum_rows": (_c.c_int, [_vp, _i64, _i32, _vp, _vp, _i32, _vp, _i64, _vp]),
     "rubix_psf_fwd": (
         _c.c_int, [_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _vp, _i32, _vp]
     ),

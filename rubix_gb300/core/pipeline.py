@@ -1,0 +1,89 @@
+"""RubixPipeline (rubix/core/pipeline.py:30-208), eager, on the rubix_gb300 kernels.
+
+Differences from rubix, all outside the particle -> cube path: the particle data is
+passed in (``data=``) instead of being read from simulation files; ``rotate_galaxy``
+expects particles already in the observer frame and ``apply_noise`` is not part of
+this package (both raise if their configuration asks for work); the SSP lookup is
+bilinear (``ssp.method = "linear"``).
+"""
+
+from __future__ import annotations
+
+import time
+from typing import Optional
+
+from ..logging import get_logger
+from ..pipeline import LinearTransformerPipeline
+from .config import get_config, get_pipeline_config
+from .data import RubixData, get_reshape_data
+from .ifu import (get_calculate_datacube, get_calculate_spectra,
+                  get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
+from .lsf import get_convolve_lsf
+from .psf import get_convolve_psf
+from .ssp import get_ssp
+from .telescope import get_filter_particles, get_spaxel_assignment, get_telescope
+
+
+def get_galaxy_rotation(config: dict):
+    """Particles are taken in the observer frame; a configured rotation is refused."""
+    rot = config.get("galaxy", {}).get("rotation")
+    if rot not in (None, {}, "none") and not (isinstance(rot, dict) and
+                                              all(float(v) == 0 for v in rot.values())):
+        raise NotImplementedError(
+            "galaxy rotation is not part of rubix_gb300: pass particles in the observer frame")
+
+    def rotate_galaxy(rubixdata: RubixData) -> RubixData:
+        return rubixdata
+
+    return rotate_galaxy
+
+
+def get_apply_noise(config: dict):
+    """Noise is not part of rubix_gb300; a configured signal-to-noise is refused."""
+    noise = config.get("telescope", {}).get("noise")
+    if noise and noise.get("signal_to_noise") not in (None, 0):
+        raise NotImplementedError("apply_noise is not part of rubix_gb300")
+
+    def apply_noise(rubixdata: RubixData) -> RubixData:
+        return rubixdata
+
+    return apply_noise
+
+
+class RubixPipeline:
+    def __init__(self, user_config, data: Optional[RubixData] = None):
+        self.user_config = get_config(user_config)
+        self.pipeline_config = get_pipeline_config(self.user_config["pipeline"]["name"])
+        self.logger = get_logger(self.user_config.get("logger"))
+        self.ssp = get_ssp(self.user_config)
+        self.telescope = get_telescope(self.user_config)
+        if data is None:
+            raise ValueError("rubix_gb300.RubixPipeline needs the particle data (data=RubixData)")
+        self.data = data
+        self.func = None
+
+    def _get_pipeline_functions(self) -> list:
+        c = self.user_config
+        return [
+            get_galaxy_rotation(c), get_filter_particles(c), get_spaxel_assignment(c),
+            get_calculate_spectra(c), get_reshape_data(c), get_scale_spectrum_by_mass(c),
+            get_doppler_shift_and_resampling(c), get_calculate_datacube(c),
+            get_convolve_psf(c), get_convolve_lsf(c), get_apply_noise(c),
+        ]
+
+    def run(self) -> RubixData:
+        t0 = time.time()
+        self._pipeline = LinearTransformerPipeline(self.pipeline_config,
+                                                   self._get_pipeline_functions())
+        self.func = self._pipeline.expression
+        out = self.func(self.data)
+        import torch
+
+        torch.cuda.synchronize()
+        self.logger.info("Pipeline run completed in %.2f seconds.", time.time() - t0)
+        return out
+
+    def gradient(self):
+        """rubix/core/pipeline.py:204-208 raises here as well; gradients of the cube are
+        available through rubix_gb300.autograd."""
+        raise NotImplementedError("Gradient calculation is not implemented yet")

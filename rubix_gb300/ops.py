@@ -158,7 +158,8 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
               _ptr(seg_offsets), int(n_segments), n,
               None if lsf is None else lsf.ctypes.data, 0 if lsf is None else lsf.size,
               int(lsf_crop), _ptr(out), out.stride(0), _ptr(ws), ws.numel(), _stream(dev))
-    _count((8 + (1 if n > 0 else 0)) if n_segments > 0 else 0)
+    # setup, corner table, prefix, count, three scans, fill, main (+ gather when n > 0)
+    _count((9 + (1 if n > 0 else 0)) if n_segments > 0 else 0)
     if check and n_segments > 0:
         import ctypes
 
@@ -203,3 +204,79 @@ def lsf_forward(cube: torch.Tensor, taps, crop: int, out=None) -> torch.Tensor:
               orow.stride(0), k.ctypes.data, k.size, int(crop), _stream(cube.device))
     _count(1 if cube.numel() > 0 else 0)
     return out
+
+
+# ------------------------------------------------------------------ materialised steps
+def ssp_lookup(ssp_flux, ssp_metallicity, ssp_age, metallicity, age, mass=None):
+    """[n, n_wave] bilinear SSP lookup (times mass when given)."""
+    ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
+    nz, na, nw = ssp_flux.shape
+    zg = _contig("ssp_metallicity", ssp_metallicity, torch.float32)
+    ag = _contig("ssp_age", ssp_age, torch.float32)
+    metallicity = _contig("metallicity", metallicity, torch.float32).reshape(-1)
+    age = _contig("age", age, torch.float32).reshape(-1)
+    if mass is not None:
+        mass = _contig("mass", mass, torch.float32).reshape(-1)
+    n = metallicity.numel()
+    out = torch.empty((n, nw), dtype=torch.float32, device=metallicity.device)
+    _lib.call("rubix_ssp_lookup", _ptr(ssp_flux), _ptr(zg), _ptr(ag), nz, na, nw,
+              _ptr(metallicity), _ptr(age), _ptr(mass), n, _ptr(out), nw,
+              _stream(metallicity.device))
+    _count(1 if n > 0 else 0)
+    return out
+
+
+def scale_rows(rows, mass):
+    """rows[i, :] * mass[i]."""
+    rows = _contig("rows", rows, torch.float32)
+    mass = _contig("mass", mass, torch.float32).reshape(-1)
+    n, nw = rows.shape
+    out = torch.empty_like(rows)
+    _lib.call("rubix_scale_rows", _ptr(rows), nw, _ptr(mass), n, nw, _ptr(out), nw,
+              _stream(rows.device))
+    _count(1 if rows.numel() > 0 else 0)
+    return out
+
+
+def resample_rows(spectra, ssp_wave_z, velocity, vel_component, wave_t):
+    """resample_spectrum of each row on its Doppler-shifted grid -> [n, L]."""
+    spectra = _contig("spectra", spectra, torch.float32)
+    wz = _contig("ssp_wave_z", ssp_wave_z, torch.float32)
+    velocity = _contig("velocity", velocity, torch.float32)
+    wave_t = _contig("wave_t", wave_t, torch.float32)
+    n, nw = spectra.shape
+    L = wave_t.numel()
+    vstride = velocity.shape[1] if velocity.dim() == 2 else 1
+    out = torch.empty((n, L), dtype=torch.float32, device=spectra.device)
+    _lib.call("rubix_resample_rows", _ptr(spectra), nw, _ptr(wz), nw, _ptr(velocity), vstride,
+              int(vel_component), n, _ptr(wave_t), L, _ptr(out), L, _stream(spectra.device))
+    _count(1 if n > 0 else 0)
+    return out
+
+
+def segment_sum_rows(rows, perm, seg_offsets, n_segments):
+    """Per-spaxel ordered sum of given rows -> [n_segments, L]."""
+    rows = _contig("rows", rows, torch.float32)
+    perm = _contig("perm", perm, torch.int32)
+    seg_offsets = _contig("seg_offsets", seg_offsets, torch.int32)
+    L = rows.shape[1]
+    out = torch.empty((int(n_segments), L), dtype=torch.float32, device=rows.device)
+    _lib.call("rubix_segment_sum_rows", _ptr(rows), L, L, _ptr(perm), _ptr(seg_offsets),
+              int(n_segments), _ptr(out), L, _stream(rows.device))
+    _count(1 if n_segments > 0 else 0)
+    return out
+
+
+def mask_zero_(values, mask):
+    """In place: values[i, ...] = 0 where mask[i] == 0 (float32, contiguous rows)."""
+    _check_cuda("values", values, torch.float32)
+    if not values.is_contiguous():
+        raise ValueError("values must be contiguous")
+    mask = _contig("mask", mask, torch.uint8).reshape(-1)
+    n = mask.numel()
+    width = values.numel() // max(n, 1) if n else 0
+    if n and values.numel() != n * width:
+        raise ValueError("values must have one row per mask entry")
+    _lib.call("rubix_mask_zero", _ptr(values), n, width, width, _ptr(mask), _stream(values.device))
+    _count(1 if values.numel() > 0 else 0)
+    return values

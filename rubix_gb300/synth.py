@@ -171,12 +171,14 @@ class Workload:
 
 
 def make_workload(name: str, n: int | None = None, edge_cases: bool = True,
-                  n_wave_t: int | None = None) -> Workload:
+                  n_wave_t: int | None = None, seed: int | None = None) -> Workload:
     """Build a named workload; ``n`` overrides the particle count, ``n_wave_t`` truncates
-    the telescope grid (for fast CPU checks)."""
-    cfg = WORKLOADS[name]
+    the telescope grid (for fast CPU checks), ``seed`` the particle seed."""
+    cfg = dict(WORKLOADS[name])
+    if seed is not None:
+        cfg["seed"] = seed
     n_age, n_met, n_wave = cfg["ssp"]
-    ssp = make_ssp(n_age, n_met, n_wave, seed=cfg["seed"])
+    ssp = make_ssp(n_age, n_met, n_wave, seed=WORKLOADS[name]["seed"])
     sbin = int(np.floor(cfg["fov"] / SPATIAL_RES))
     edges, _ = tel.spatial_bin_edges(cfg["fov"], sbin, DIST_Z)
     gal = make_galaxy(cfg["n"] if n is None else n, seed=cfg["seed"],

@@ -1,0 +1,152 @@
+"""The rubix-compatible step API on the GPU against the oracle, step by step and as a
+whole pipeline, plus rubix's known-answer cases run through the CUDA kernels."""
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import assert_cube_close, oracle_stages, to_dev, workload
+
+pytestmark = pytest.mark.gpu
+
+
+def _config(w, name="small_test_ssp"):
+    from rubix_gb300.core import register_ssp_template
+    from rubix_gb300.core.ssp import SSPGrid
+
+    register_ssp_template(name, SSPGrid(age=w.ssp.age, metallicity=w.ssp.metallicity,
+                                        wavelength=w.ssp.wavelength, flux=w.ssp.flux))
+    return {
+        "pipeline": {"name": "calc_ifu"},
+        "logger": {"log_level": "WARNING"},
+        "data": {"args": {"particle_type": ["stars"]}},
+        "telescope": {"name": "MUSE", "psf": {"name": "gaussian", "size": w.psf_size,
+                                              "sigma": w.psf_sigma},
+                      "lsf": {"sigma": w.lsf_sigma}},
+        "cosmology": {"name": "PLANCK15"},
+        "galaxy": {"dist_z": w.dist_z},
+        "ssp": {"template": {"name": name}, "method": "linear"},
+    }
+
+
+def _data(w):
+    from rubix_gb300.core import RubixData, StarsData
+
+    p = w.particles
+    return RubixData(stars=StarsData(coords=p.coords.copy(), velocity=p.velocity.copy(),
+                                     mass=p.mass.copy(), metallicity=p.metallicity.copy(),
+                                     age=p.age.copy()))
+
+
+def test_rubix_pipeline_matches_oracle():
+    from rubix_gb300.core import RubixPipeline
+
+    w = workload("small")
+    ref = oracle_stages("small")
+    out = RubixPipeline(_config(w), _data(w)).run()
+    cube = out.stars.datacube.cpu().numpy()
+    assert cube.shape == (25, 25, 3721)
+    assert_cube_close(cube, ref["final"], what="RubixPipeline cube")
+    assert np.array_equal(out.stars.pixel_assignment.cpu().numpy().reshape(-1),
+                          ref["pixel_assignment"])
+    assert np.array_equal(out.stars.mask.cpu().numpy().reshape(-1), ref["mask"])
+
+
+def test_steps_one_by_one_materialised():
+    import torch
+
+    from rubix_gb300 import core
+
+    w = workload("small", n=600)
+    cfg = _config(w, "small600")
+    p = w.particles
+    d = _data(w)
+    d = core.get_filter_particles(cfg)(d)
+    mask, f = oracle.filter_particles(p.coords, w.edges, mass=p.mass, metallicity=p.metallicity,
+                                      age=p.age)
+    assert np.array_equal(d.stars.mass.cpu().numpy().reshape(-1), f["mass"])
+    assert np.array_equal(d.stars.age.cpu().numpy().reshape(-1), f["age"])
+    d = core.get_spaxel_assignment(cfg)(d)
+    d = core.get_reshape_data(cfg)(d)
+    assert d.stars.mass.shape == (1, p.n) and d.stars.coords.shape == (1, p.n, 3)
+    d = core.get_calculate_spectra(cfg)(d)
+    lookup = oracle.interp2d_linear(f["metallicity"], f["age"], w.ssp.metallicity, w.ssp.age,
+                                    w.ssp.flux)
+    got = np.asarray(d.stars.spectra)
+    assert got.shape == (1, p.n, w.ssp.wavelength.size)
+    assert_cube_close(got[0], lookup, what="lookup spectra")
+    d = core.get_scale_spectrum_by_mass(cfg)(d)
+    assert_cube_close(np.asarray(d.stars.spectra)[0], lookup * f["mass"][:, None],
+                      what="mass-scaled spectra")
+    d = core.get_doppler_shift_and_resampling(cfg)(d)
+    want = oracle.particle_spectra(f["mass"], f["metallicity"], f["age"], p.velocity[:, 2],
+                                   w.ssp.metallicity, w.ssp.age, w.ssp.flux, w.wave_z, w.wave_t)
+    res = np.asarray(d.stars.spectra)
+    assert res.shape == (1, p.n, w.wave_t.size)
+    assert_cube_close(res[0], want, what="resampled spectra")
+    lazy = core.get_calculate_datacube(cfg)(d).stars.datacube.cpu().numpy()
+    ref_cube = oracle.calculate_cube(want, oracle.square_spaxel_assignment(p.coords, w.edges),
+                                     w.sbin)
+    assert_cube_close(lazy, ref_cube, what="lazy datacube")
+    # the same step on materialised spectra (segment-sum path)
+    d.stars.spectra = torch.as_tensor(res).cuda()
+    mat = core.get_calculate_datacube(cfg)(d).stars.datacube.cpu().numpy()
+    assert_cube_close(mat, ref_cube, what="datacube from materialised spectra")
+
+
+def test_doppler_step_on_given_spectra():
+    """doppler_shift_and_resampling applied to spectra the caller supplies."""
+    import torch
+
+    from rubix_gb300 import core
+
+    w = workload("small", n=300)
+    cfg = _config(w, "small300")
+    p = w.particles
+    rng = np.random.default_rng(4)
+    spec = (rng.random((p.n, w.ssp.wavelength.size)) + 0.1).astype(np.float32)
+    d = _data(w)
+    d.stars.spectra = torch.as_tensor(spec[None]).cuda()
+    d = core.get_doppler_shift_and_resampling(cfg)(d)
+    lp = oracle.velocity_doppler_shift32(w.wave_z, p.velocity[:, 2])
+    want, _ = oracle.resample_spectra(spec, lp, w.wave_t)
+    assert_cube_close(d.stars.spectra.cpu().numpy()[0], want, what="resample_rows")
+
+
+def test_known_answers_on_gpu():
+    import torch
+
+    from rubix_gb300 import ops
+
+    # calculate_cube, rubix tests/test_spectra_ifu.py:231-257
+    spectra = to_dev(np.array([[100, 200, 300], [400, 500, 600], [700, 800, 900], [1, 2, 3]],
+                              dtype=np.float32))
+    perm, offs = ops.spaxel_sort(to_dev(np.array([0, 1, 1, 3], dtype=np.int32)), 4)
+    cube = ops.segment_sum_rows(spectra, perm, offs, 4).reshape(2, 2, 3).cpu().numpy()
+    assert np.array_equal(cube, [[[100, 200, 300], [1100, 1300, 1500]], [[0, 0, 0], [1, 2, 3]]])
+    # resample_spectrum, rubix tests/test_spectra_ifu.py:175-228 (zero velocity)
+    F = np.array([[1.0, 2.0, 3.0, 4.0, 5.0], [0, 0, 0, 0, 0]], dtype=np.float32)
+    lam = np.array([4000.0, 5000.0, 6000.0, 7000.0, 8000.0], dtype=np.float32)
+    lt = np.array([4500.0, 5500.0, 6500.0, 7500.0], dtype=np.float32)
+    got = ops.resample_rows(to_dev(F), to_dev(lam), to_dev(np.zeros((2, 3), np.float32)), 2,
+                            to_dev(lt)).cpu().numpy()
+    np.testing.assert_allclose(got[0], oracle.resample_spectrum(F[0], lam, lt), rtol=1e-5)
+    assert (got[1] == 0).all() and not np.isnan(got).any()
+    # apply_lsf delta, rubix tests/test_telescope_lsf.py:6-60
+    from rubix_gb300 import telescope as tel
+
+    sp = np.zeros((3, 100), dtype=np.float32)
+    for i, pos in enumerate([20, 50, 75]):
+        sp[i, pos] = 1.0
+    out = ops.lsf_forward(to_dev(sp), tel.lsf_taps(2.0, 1.0), 12).cpu().numpy()
+    x = np.arange(100)
+    for i, pos in enumerate([20, 50, 75]):
+        g = np.exp(-0.5 * (x - pos) ** 2 / 4.0)
+        np.testing.assert_allclose(out[i], g / g.sum(), atol=1e-5)
+    # apply_psf with a 3x3 ones kernel, rubix tests/test_telescope_psf.py:21-54
+    c = np.zeros((10, 10, 3), dtype=np.float32)
+    c[5, 5, :] = 1.0
+    o = ops.psf_forward(to_dev(c), np.ones(3)).cpu().numpy()
+    want = oracle.apply_psf(c, np.ones((3, 3)))
+    np.testing.assert_allclose(o, want, atol=1e-6)
+    torch.cuda.synchronize()
