@@ -251,6 +251,50 @@ RUBIX_API int rubix_lsf_fwd(const float* in, float* out, int64_t n_rows, int32_t
                   int64_t row_stride_in, int64_t row_stride_out, const float* taps,
                   int32_t n_taps, int32_t crop, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Adjoints (gradients of a loss L of the cube)                              */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * The gradient of the datacube with respect to the particle inputs that rubix
+ * obtains with jax.grad through calculate_spectra -> scale_spectrum_by_mass ->
+ * doppler_shift_and_resampling -> calculate_datacube (rubix/core/ifu.py:29-341;
+ * RubixPipeline.gradient, rubix/core/pipeline.py:204-208).
+ * adj[s][t] (row stride adj_stride) = dL/dcube[s][t] of the cube rubix_cube_fwd
+ * writes WITHOUT its LSF epilogue (apply the PSF and LSF adjoints to dL/dcube first:
+ * rubix_psf_fwd / rubix_lsf_fwd with reversed taps).  Writes, for every particle
+ * i < n (zero for particles outside the sorted set), dL/dmass_i, dL/dmetallicity_i,
+ * dL/dage_i and dL/dv_i of the line-of-sight velocity component; any of the four
+ * output pointers may be NULL.  Derivatives hold the float32 bracket choices and the
+ * in-range wavelength mask fixed, as automatic differentiation of the forward
+ * formulas does; particles with T' = 0 or a non-finite T/T' get zero gradients.
+ * Same inputs and limits as rubix_cube_fwd; deterministic.
+ */
+RUBIX_API size_t rubix_cube_bwd_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
+                                               int32_t n_met, int32_t n_age, int32_t n_wave);
+RUBIX_API int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicity,
+                             const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                             int32_t n_age, int32_t n_wave, const float* wave_t,
+                             int32_t n_wave_t, const float* mass, const float* metallicity,
+                             const float* age, const float* velocity, int64_t vel_stride,
+                             int32_t vel_component, const int32_t* perm,
+                             const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                             const float* adj, int64_t adj_stride, float* grad_mass,
+                             float* grad_metallicity, float* grad_age, float* grad_vlos,
+                             void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * No counterpart in rubix (jax.grad reduces inside XLA).
+ * *out (device double) = sum_i a[i] * b[i]: per-thread float partial sums, double
+ * block and grid reductions in a fixed order (deterministic).  Used for the
+ * gradients with respect to the PSF and LSF widths, <dL/dcube, d cube/d sigma>.
+ * The workspace (rubix_dot_workspace_size bytes, 8-byte aligned) must not be shared
+ * by calls in flight at the same time.
+ */
+RUBIX_API size_t rubix_dot_workspace_size(void);
+RUBIX_API int rubix_dot(const float* a, const float* b, int64_t n, double* out, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,7 +157,7 @@ def filter_particles(coords, edges, **arrays):
 # ----------------------------------------------------------------------------------
 # SSP lookup: interpax.interp2d(method="linear", extrap=0), spectra/ssp/grid.py:113-120
 # ----------------------------------------------------------------------------------
-def interp2d_linear(xq, yq, x, y, f):
+def interp2d_linear(xq, yq, x, y, f, query_dtype=np.float32):
     """Bilinear interpolation of ``f[x, y, :]`` at ``(xq, yq)``; 0 outside the box.
 
     Restates interpax's linear branch: cell ``i = clip(searchsorted(x, xq, 'right'),
@@ -166,8 +166,8 @@ def interp2d_linear(xq, yq, x, y, f):
     ``yq < y[0]`` or ``yq > y[-1]`` (boundaries inclusive).  In rubix ``x`` is the
     metallicity grid and ``y`` the age grid (grid.py:113-120; flux layout [Z, age, lambda]).
     """
-    xq = np.asarray(xq, dtype=np.float32).astype(np.float64)
-    yq = np.asarray(yq, dtype=np.float32).astype(np.float64)
+    xq = np.asarray(xq, dtype=query_dtype).astype(np.float64)
+    yq = np.asarray(yq, dtype=query_dtype).astype(np.float64)
     x = np.asarray(x, dtype=np.float32).astype(np.float64)
     y = np.asarray(y, dtype=np.float32).astype(np.float64)
     f = np.asarray(f, dtype=np.float32).astype(np.float64)
@@ -452,6 +452,154 @@ def cube_rel_error(test, ref, rel_floor=1e-3):
 
 
 __all__ += ["cube_rel_error"]
+
+
+# ----------------------------------------------------------------------------------
+# Gradients (rubix differentiates the same chain with jax.grad,
+# RubixPipeline.gradient, core/pipeline.py:204-208)
+# ----------------------------------------------------------------------------------
+def interp2d_linear_grad(xq, yq, x, y, f, query_dtype=np.float32):
+    """``interp2d_linear`` and its derivatives with respect to ``xq`` (metallicity) and
+    ``yq`` (age) inside the containing cell; all three are 0 outside the box."""
+    xq = np.asarray(xq, dtype=query_dtype).astype(np.float64)
+    yq = np.asarray(yq, dtype=query_dtype).astype(np.float64)
+    x = np.asarray(x, dtype=np.float32).astype(np.float64)
+    y = np.asarray(y, dtype=np.float32).astype(np.float64)
+    f = np.asarray(f, dtype=np.float32).astype(np.float64)
+    i = np.clip(np.searchsorted(x, xq, side="right"), 1, len(x) - 1)
+    j = np.clip(np.searchsorted(y, yq, side="right"), 1, len(y) - 1)
+    dx = x[i] - x[i - 1]
+    dy = y[j] - y[j - 1]
+    tx = np.where(dx == 0, 0.0, (xq - x[i - 1]) / np.where(dx == 0, 1.0, dx))[:, None]
+    ty = np.where(dy == 0, 0.0, (yq - y[j - 1]) / np.where(dy == 0, 1.0, dy))[:, None]
+    ix = np.where(dx == 0, 0.0, 1.0 / np.where(dx == 0, 1.0, dx))[:, None]
+    iy = np.where(dy == 0, 0.0, 1.0 / np.where(dy == 0, 1.0, dy))[:, None]
+    f00, f10, f01, f11 = f[i - 1, j - 1], f[i, j - 1], f[i - 1, j], f[i, j]
+    fq = (1 - tx) * (1 - ty) * f00 + tx * (1 - ty) * f10 + (1 - tx) * ty * f01 + tx * ty * f11
+    fx = ix * ((1 - ty) * (f10 - f00) + ty * (f11 - f01))
+    fy = iy * ((1 - tx) * (f01 - f00) + tx * (f11 - f10))
+    outside = (xq < x[0]) | (xq > x[-1]) | (yq < y[0]) | (yq > y[-1])
+    for a in (fq, fx, fy):
+        a[outside] = 0.0
+    return fq, fx, fy
+
+
+def _interp_rows_slope(lt, lp, F):
+    """``_interp_rows`` plus the slope dI/dlambda' of the bracket used (0 where the
+    value is clamped to an end of the row)."""
+    n, nl = lp.shape
+    i = np.empty((n, lt.shape[0]), dtype=np.int64)
+    for r in range(n):
+        i[r] = np.searchsorted(lp[r], lt, side="right")
+    ic = np.clip(i, 1, nl - 1)
+    x0 = np.take_along_axis(lp, ic - 1, axis=1)
+    x1 = np.take_along_axis(lp, ic, axis=1)
+    f0 = np.take_along_axis(F, ic - 1, axis=1)
+    f1 = np.take_along_axis(F, ic, axis=1)
+    dx = x1 - x0
+    slope = np.where(dx == 0, 0.0, (f1 - f0) / np.where(dx == 0, 1.0, dx))
+    val = f0 + (lt[None, :] - x0) * slope
+    lo = lt[None, :] < lp[:, :1]
+    hi = lt[None, :] > lp[:, -1:]
+    val = np.where(lo, F[:, :1], np.where(hi, F[:, -1:], val))
+    slope = np.where(lo | hi, 0.0, slope)
+    return val, slope
+
+
+def doppler_grid(wave_z, v_los, smooth=False):
+    """The shifted SSP grid: float32 like the reference, or (``smooth``) float64
+    ``lambda_z * exp(v/c)`` for finite differences in v."""
+    if not smooth:
+        return velocity_doppler_shift32(wave_z, v_los).astype(np.float64)
+    v = np.asarray(v_los, dtype=np.float64)
+    return np.asarray(wave_z, dtype=np.float32).astype(np.float64)[None, :] * np.exp(
+        v / SPEED_OF_LIGHT)[:, None]
+
+
+def particle_objective(mass, metallicity, age, v_los, ssp_metallicity, ssp_age, ssp_flux,
+                       wave_z, wave_t, adj_rows, smooth=True):
+    """``sum_t adj_rows[p, t] * c_p[t]`` per particle, with ``c_p`` the resampled,
+    mass-scaled spectrum of ``particle_spectra``.  With ``smooth`` the shifted grid and
+    the (metallicity, age) queries stay float64, for finite differences."""
+    qd = np.float64 if smooth else np.float32
+    G = interp2d_linear(metallicity, age, ssp_metallicity, ssp_age, ssp_flux, query_dtype=qd)
+    m = np.asarray(mass, dtype=np.float64)
+    lp = doppler_grid(wave_z, v_los, smooth)
+    lt = np.asarray(wave_t, dtype=np.float32).astype(np.float64)
+    in_range = (lp >= lt.min()) & (lp <= lt.max())
+    T = np.sum(G * calculate_diff(lp) * in_range, axis=1)
+    I = _interp_rows(lt, lp, G)
+    Tp = np.sum(I * calculate_diff(lt)[None, :], axis=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = _nan_to_num32(T / Tp)
+    return m * s * np.sum(np.asarray(adj_rows, dtype=np.float64) * I, axis=1)
+
+
+def particle_grads(mass, metallicity, age, v_los, ssp_metallicity, ssp_age, ssp_flux,
+                   wave_z, wave_t, adj_rows, smooth=False):
+    """Analytic d/d(mass, metallicity, age, v_los) of ``particle_objective``: the
+    derivative of the forward formulas (core/ifu.py:63-295, spectra/ifu.py:168-266)
+    with the interpolation brackets and the in-range mask held fixed.  With
+    beta = m T / T' and gamma = sum_t a_t I_t:
+        d/dm = (T/T') gamma,
+        d/dtheta = beta H_theta + gamma (m/T') (dT/dtheta - (T/T') dT'/dtheta),
+    H_theta = sum_t a_t dI_t/dtheta; dI_t/dv = -lambda_t * slope_t / c, dT/dv = T/c.
+    Particles with T' = 0 or a non-finite T/T' get zeros.  Returns four (n,) arrays."""
+    m = np.asarray(mass, dtype=np.float64)
+    qd = np.float64 if smooth else np.float32
+    G, GZ, GA = interp2d_linear_grad(metallicity, age, ssp_metallicity, ssp_age, ssp_flux,
+                                     query_dtype=qd)
+    lp = doppler_grid(wave_z, v_los, smooth)
+    lt = np.asarray(wave_t, dtype=np.float32).astype(np.float64)
+    a = np.asarray(adj_rows, dtype=np.float64)
+    in_range = (lp >= lt.min()) & (lp <= lt.max())
+    dlp = calculate_diff(lp) * in_range
+    dlt = calculate_diff(lt)[None, :]
+    T, TZ, TA = (np.sum(X * dlp, axis=1) for X in (G, GZ, GA))
+    I, slope = _interp_rows_slope(lt, lp, G)
+    IZ = _interp_rows(lt, lp, GZ)
+    IA = _interp_rows(lt, lp, GA)
+    Iv = -lt[None, :] * slope / SPEED_OF_LIGHT
+    Tp = np.sum(I * dlt, axis=1)
+    gamma = np.sum(a * I, axis=1)
+    H = {k: np.sum(a * X, axis=1) for k, X in (("Z", IZ), ("A", IA), ("v", Iv))}
+    D = {k: np.sum(dlt * X, axis=1) for k, X in (("Z", IZ), ("A", IA), ("v", Iv))}
+    dT = {"Z": TZ, "A": TA, "v": T / SPEED_OF_LIGHT}
+    with np.errstate(divide="ignore", invalid="ignore"):
+        sc = T / Tp
+        ok = (Tp != 0) & np.isfinite(sc)
+        sc = np.where(ok, sc, 0.0)
+        k = np.where(ok, m / np.where(Tp == 0, 1.0, Tp), 0.0)
+    beta = m * sc
+    out = [np.where(ok, sc * gamma, 0.0)]
+    for key in ("Z", "A", "v"):
+        out.append(np.where(ok, beta * H[key] + gamma * k * (dT[key] - sc * D[key]), 0.0))
+    return tuple(out)
+
+
+def psf_taps_derivative(m, sigma):
+    """1-D PSF taps t (normalised Gaussian of ``gaussian_kernel_2d``) and dt/dsigma."""
+    x = np.arange(-((m - 1) / 2), ((m - 1) / 2) + 1)
+    e = np.exp(-(x**2) / (2 * sigma**2))
+    de = e * x**2 / sigma**3
+    S = e.sum()
+    t = e / S
+    return t, (de - t * de.sum()) / S
+
+
+def lsf_taps_derivative(sigma, wave_res, factor=12):
+    """``lsf_kernel`` taps and their derivative with respect to sigma."""
+    x = np.arange(-factor * wave_res, factor * wave_res + wave_res, wave_res,
+                  dtype=np.float32).astype(np.float64)
+    e = np.exp(-0.5 * x**2 / sigma**2)
+    de = e * x**2 / sigma**3
+    S = e.sum()
+    t = e / S
+    return t, (de - t * de.sum()) / S
+
+
+__all__ += ["interp2d_linear_grad", "doppler_grid", "particle_objective", "particle_grads",
+            "psf_taps_derivative", "lsf_taps_derivative"]
 
 
 def _selftest():  # pragma: no cover - manual helper

@@ -63,6 +63,17 @@ SIGNATURES = {
         _c.c_int, [_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _vp, _i32, _vp]
     ),
     "rubix_lsf_fwd": (_c.c_int, [_vp, _vp, _i64, _i32, _i64, _i64, _vp, _i32, _i32, _vp]),
+    "rubix_cube_bwd_workspace_size": (_sz, [_i64, _i32, _i32, _i32, _i32, _i32]),
+    "rubix_cube_bwd": (
+        _c.c_int,
+        [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32,
+         _vp, _vp, _vp, _vp, _i64, _i32,
+         _vp, _vp, _i32, _i64,
+         _vp, _i64, _vp, _vp, _vp, _vp,
+         _vp, _sz, _vp],
+    ),
+    "rubix_dot_workspace_size": (_sz, []),
+    "rubix_dot": (_c.c_int, [_vp, _vp, _i64, _vp, _vp, _sz, _vp]),
 }
 
 _lock = threading.Lock()

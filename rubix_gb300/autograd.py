@@ -1,0 +1,145 @@
+"""Gradients of the datacube with respect to the particles and the PSF/LSF widths.
+
+rubix differentiates its pipeline with ``jax.grad`` (``RubixPipeline.gradient``,
+rubix/core/pipeline.py:204-208): the cube is a differentiable function of the particle
+masses, metallicities, ages and velocities and of the telescope's PSF and LSF widths.
+``DatacubeFunction`` is the same function as a ``torch.autograd.Function`` over the
+CUDA kernels:
+
+    forward   A    = rubix_cube_fwd(particles)            (no LSF epilogue; kept)
+              Q    = rubix_lsf_fwd(A, lsf taps(sigma_lsf)) (kept)
+              cube = rubix_psf_fwd(Q, psf taps(sigma_psf))
+    backward  gP   = PSF^T g,  h = LSF^T gP                (convolutions with reversed taps)
+              particle gradients = rubix_cube_bwd(h)
+              dL/dsigma_psf = <g, PSF_{dt x t}(Q)> + <g, PSF_{t x dt}(Q)>
+              dL/dsigma_lsf = <gP, LSF_{dt}(A)>
+
+The PSF and LSF act on different axes and commute, so the forward cube equals
+rubix's convolve_psf followed by convolve_lsf.  Gradients flow to the particle
+inputs (velocity: the line-of-sight component only) and to ``sigma_psf`` /
+``sigma_lsf`` given as tensors; the spaxel assignment (coordinates) is piecewise
+constant and gets none, as in rubix.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import ops
+from . import telescope as tel
+
+__all__ = ["DatacubeFunction", "render_cube", "psf_taps_grad", "lsf_taps_grad"]
+
+
+def psf_taps_grad(m: int, sigma: float):
+    """1-D PSF taps (gaussian_kernel_2d(m, m, sigma) is their outer product) and their
+    derivative with respect to sigma, float64."""
+    x = np.arange(-((m - 1) / 2), ((m - 1) / 2) + 1)
+    e = np.exp(-(x**2) / (2 * sigma**2))
+    de = e * x**2 / sigma**3
+    S = e.sum()
+    t = e / S
+    return t, (de - t * de.sum()) / S
+
+
+def lsf_taps_grad(sigma: float, wave_res: float, factor: int = 12):
+    """LSF taps of rubix/telescope/lsf/lsf.py:12-26 and their derivative, float64."""
+    x = np.arange(-factor * wave_res, factor * wave_res + wave_res, wave_res,
+                  dtype=np.float32).astype(np.float64)
+    e = np.exp(-0.5 * x**2 / sigma**2)
+    de = e * x**2 / sigma**3
+    S = e.sum()
+    t = e / S
+    return t, (de - t * de.sum()) / S
+
+
+def _psf_adjoint_taps(t: np.ndarray) -> np.ndarray:
+    """Taps whose 'same' convolution (centre (m-1)//2) is the adjoint of the 'same'
+    convolution with ``t``: reversed, plus a trailing zero for even m."""
+    r = np.asarray(t, dtype=np.float64)[::-1]
+    return r if r.size % 2 == 1 else np.concatenate([r, [0.0]])
+
+
+def _scalar(x) -> float:
+    return float(x.detach().item()) if isinstance(x, torch.Tensor) else float(x)
+
+
+class DatacubeFunction(torch.autograd.Function):
+    """cube [sbin, sbin, L] = PSF(LSF(accumulate(mass, metallicity, age, velocity))).
+
+    ``renderer`` is an ``IFURenderer`` (SSP grid, wavelength grids, bins, velocity
+    axis); ``perm`` / ``seg_offsets`` its sort of the particles; ``psf_size`` the PSF
+    kernel width in spaxels and ``wave_res`` the telescope wavelength step (LSF taps).
+    """
+
+    @staticmethod
+    def forward(ctx, mass, metallicity, age, velocity, sigma_psf, sigma_lsf, renderer, perm,
+                seg_offsets, psf_size, wave_res):
+        r = renderer
+        nseg = r.sbin * r.sbin
+        A = ops.cube_forward(r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t,
+                             mass, metallicity, age, velocity, r.velocity_axis, perm,
+                             seg_offsets, nseg)
+        sp, sl = _scalar(sigma_psf), _scalar(sigma_lsf)
+        tl, _ = lsf_taps_grad(sl, wave_res)
+        crop = (tl.size - 1) // 2
+        Q = ops.lsf_forward(A, tl, crop)
+        tp, _ = psf_taps_grad(int(psf_size), sp)
+        cube = ops.psf_forward(Q.view(r.sbin, r.sbin, -1), tp)
+        ctx.save_for_backward(mass, metallicity, age, velocity, A, Q)
+        ctx.r = r
+        ctx.perm, ctx.seg_offsets = perm, seg_offsets
+        ctx.sp, ctx.sl, ctx.psf_size, ctx.wave_res = sp, sl, int(psf_size), wave_res
+        ctx.sigma_dtypes = (
+            sigma_psf.dtype if isinstance(sigma_psf, torch.Tensor) else None,
+            sigma_lsf.dtype if isinstance(sigma_lsf, torch.Tensor) else None)
+        return cube
+
+    @staticmethod
+    def backward(ctx, g):
+        mass, metallicity, age, velocity, A, Q = ctx.saved_tensors
+        r = ctx.r
+        nseg = r.sbin * r.sbin
+        g = g.contiguous().float()
+        tp, dtp = psf_taps_grad(ctx.psf_size, ctx.sp)
+        tl, dtl = lsf_taps_grad(ctx.sl, ctx.wave_res)
+        crop = (tl.size - 1) // 2
+        gP = ops.psf_forward(g, _psf_adjoint_taps(tp))
+        need = ctx.needs_input_grad
+        grads = [None] * 11
+        if any(need[:4]):
+            h = ops.lsf_forward(gP, tl[::-1].copy(), tl.size - 1 - crop)
+            gm, gz, ga, gv = ops.cube_backward(
+                r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t, mass,
+                metallicity, age, velocity, r.velocity_axis, ctx.perm, ctx.seg_offsets, nseg,
+                h.view(nseg, -1))
+            grads[0] = gm.view_as(mass).to(mass.dtype) if need[0] else None
+            grads[1] = gz.view_as(metallicity).to(metallicity.dtype) if need[1] else None
+            grads[2] = ga.view_as(age).to(age.dtype) if need[2] else None
+            if need[3]:
+                gvel = torch.zeros_like(velocity)
+                if velocity.dim() == 2:
+                    gvel[:, r.velocity_axis] = gv.to(velocity.dtype)
+                else:
+                    gvel.copy_(gv.view_as(velocity))
+                grads[3] = gvel
+        if need[4]:
+            Qc = Q.view(r.sbin, r.sbin, -1)
+            d = ops.dot(g, ops.psf_forward(Qc, dtp, tp)) + ops.dot(g, ops.psf_forward(Qc, tp, dtp))
+            grads[4] = d.to(ctx.sigma_dtypes[0] or torch.float32)
+        if need[5]:
+            d = ops.dot(gP.view(nseg, -1), ops.lsf_forward(A, dtl, crop))
+            grads[5] = d.to(ctx.sigma_dtypes[1] or torch.float32)
+        return tuple(grads)
+
+
+def render_cube(renderer, coords, velocity, mass, metallicity, age, sigma_psf, sigma_lsf,
+                psf_size: int, wave_res: float):
+    """Differentiable datacube of one galaxy: aperture filter, spaxel sort (no
+    gradient) and ``DatacubeFunction``.  All particle tensors must be CUDA tensors;
+    ``sigma_psf`` / ``sigma_lsf`` are tensors (or floats when no gradient is wanted)."""
+    idx, mask = renderer.assign(coords)
+    perm, offs = renderer.sort(idx, mask)
+    return DatacubeFunction.apply(mass, metallicity, age, velocity, sigma_psf, sigma_lsf,
+                                  renderer, perm, offs, psf_size, wave_res)

@@ -1,0 +1,472 @@
+// Adjoint of kernel (b): gradients of L with respect to each particle's mass,
+// metallicity, age and line-of-sight velocity, given A = dL/d(cube before PSF and LSF).
+//
+// A particle p in spaxel s adds c_t = beta * I_t to the cube, with I_t the
+// interpolated mixed template on the telescope grid, beta = m * T / T'
+// (rubix/spectra/ifu.py:224-266) and T' = sum_t I_t dlambda_t.  So
+//   dL/dm     = (T / T') * gamma,                     gamma = sum_t A[s,t] I_t
+//   dL/dtheta = beta * H_theta + gamma * (m / T') * (dT/dtheta - (T / T') * D_theta)
+// for theta in {Z, age, v}, with H_theta = sum_t A[s,t] dI_t/dtheta and
+// D_theta = sum_t dlambda_t dI_t/dtheta (= dT'/dtheta).  dI/dZ and dI/dage are the
+// interpolants of the bilinear weights' derivatives applied to the four corner
+// spectra; lambda'_k = lambda_z,k * exp(v/c) gives dI_t/dv = -lambda_t * slope_k / c,
+// and dT/dv = T / c.  dT/dZ and dT/dage come from the prefix sums in the gather.
+// These are the derivatives of the forward formulas with the float32 bracket choices
+// and the in-range mask held fixed, as an automatic differentiation of them gives.
+//
+// Same decomposition as the forward kernel (persistent blocks pulling spaxel chunks,
+// TMA-staged corner-table segments, per-particle rows built in shared memory, thread i
+// owning R consecutive telescope wavelengths), one particle per step: each thread
+// accumulates 8 partial sums over its wavelengths, the block reduces them in a fixed
+// order, and warp 0 writes the particle's gradients.  No atomics, deterministic.
+#include "cube_common.cuh"
+#include "tma.cuh"
+
+namespace rubix {
+namespace {
+
+constexpr int kAdjThreads = kAccThreads;
+constexpr int kAdjWarps = kAdjThreads / 32;
+constexpr int kAdjSums = 8;
+
+struct AdjArgs {
+  const float4* ct;
+  const float* wave_z;
+  int nZ, nA, n_wave;
+  const float* zg;
+  const float* ag;
+  const float* wave_t;
+  const float* At;
+  int n_t;
+  const ParticleRec* rec;
+  const int* seg_off;
+  const int* perm;
+  const int2* items;
+  const float* adj;
+  long long adj_stride;
+  float* g_mass;
+  float* g_met;
+  float* g_age;
+  float* g_vlos;
+  CubeCtrl* ctrl;
+  const int2* bucket;
+  int row_cap;
+};
+
+struct AdjSmem {
+  size_t wz, bucket, grid, stage, row_a, row_b, red, rec, total;
+};
+
+__host__ __device__ inline AdjSmem adj_smem_layout(int n_wave, int n_grid, int row_cap) {
+  AdjSmem L;
+  size_t o = 0;
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  L.wz = o;     o = al(o + sizeof(float) * n_wave);
+  L.bucket = o; o = al(o + sizeof(int2) * kBuckets);
+  L.grid = o;   o = al(o + sizeof(float) * n_grid);
+  L.stage = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
+  L.row_a = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
+  L.row_b = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
+  L.red = o;    o = al(o + sizeof(float) * 2 * kAdjWarps * kAdjSums);
+  L.rec = o;    o = al(o + sizeof(ParticleRec) * kChunk);
+  L.total = o;
+  return L;
+}
+
+// Thread 0: bulk copy of the particle's corner-table segment (its bracket range).
+__device__ __forceinline__ void adj_issue(const AdjArgs& a, const ParticleRec& r, float4* stage,
+                                          uint64_t* bar) {
+  fence_proxy_async_smem();
+  const int4 b = r.b;
+  const int ks = b.y, ke = b.z & ~kGenericFlag;
+  const int klo = max(ks, 0);
+  const int nk = min(ke + 1, a.n_wave - 1) - klo + 1;
+  const uint32_t bytes = b.x >= 0 ? 16u * (uint32_t)nk : 0u;
+  mbar_arrive_expect_tx(bar, bytes);
+  if (b.x >= 0) bulk_copy_g2s(stage, a.ct + (long long)b.x * a.n_wave + klo, bytes, bar);
+}
+
+// Row entry e (SSP index k = kstart + e): row_a = (lambda'_k, slope, G_k, lambda'_{k+1}),
+// row_b = (GZ_k, slopeZ, GA_k, slopeA) with GZ = dG/dZ, GA = dG/dage; sentinels as in
+// the forward rows (k = -1: lambda' = -FLT_MAX, value G_0, slope 0; k >= nW-1: slope 0).
+__device__ __forceinline__ void adj_build(const AdjArgs& a, const ParticleRec& r,
+                                          const float* __restrict__ s_wz,
+                                          const float* __restrict__ s_grid,
+                                          const float4* __restrict__ stage,
+                                          float4* __restrict__ row_a, float4* __restrict__ row_b,
+                                          int lane, int warp) {
+  const int nW = a.n_wave;
+  const float tz = r.a.w, ta = __int_as_float(r.b.w), alpha = r.a.y;
+  const int ks = r.b.y, ke = r.b.z & ~kGenericFlag;
+  const int klo = max(ks, 0), khi = min(ke + 1, nW - 1);
+  const int n_e = ke - ks + 1;
+  const int cell = r.b.x;
+  const bool has_cell = cell >= 0;
+  float w00 = 0.f, w10 = 0.f, w01 = 0.f, w11 = 0.f, z0 = 0.f, z1 = 0.f, a0 = 0.f, a1 = 0.f;
+  if (has_cell) {
+    const int iz = cell / (a.nA - 1), ia = cell - iz * (a.nA - 1);
+    const float dz = s_grid[iz + 1] - s_grid[iz];
+    const float da = s_grid[a.nZ + ia + 1] - s_grid[a.nZ + ia];
+    const float izw = dz == 0.f ? 0.f : 1.f / dz, iaw = da == 0.f ? 0.f : 1.f / da;
+    w00 = (1.f - tz) * (1.f - ta);
+    w10 = tz * (1.f - ta);
+    w01 = (1.f - tz) * ta;
+    w11 = tz * ta;
+    z0 = (1.f - ta) * izw;  // GZ = z0 (F10 - F00) + z1 (F11 - F01)
+    z1 = ta * izw;
+    a0 = (1.f - tz) * iaw;  // GA = a0 (F01 - F00) + a1 (F11 - F10)
+    a1 = tz * iaw;
+  }
+  const float4* st = stage - klo;
+  for (int base = warp * 31; base < n_e; base += kAdjWarps * 31) {
+    const int e = base + lane;
+    const int k = ks + e;
+    const int kk = min(max(k, klo), khi);
+    float G = 0.f, GZ = 0.f, GA = 0.f;
+    if (has_cell) {
+      const float4 c = st[kk];
+      G = w00 * c.x;
+      G = fmaf(w10, c.y, G);
+      G = fmaf(w01, c.z, G);
+      G = fmaf(w11, c.w, G);
+      GZ = fmaf(z0, c.y - c.x, z1 * (c.w - c.z));
+      GA = fmaf(a0, c.z - c.x, a1 * (c.w - c.y));
+    }
+    const float lp = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(s_wz[k], alpha));
+    const float lp_next = __shfl_down_sync(0xffffffffu, lp, 1);
+    const float G_next = __shfl_down_sync(0xffffffffu, G, 1);
+    const float GZ_next = __shfl_down_sync(0xffffffffu, GZ, 1);
+    const float GA_next = __shfl_down_sync(0xffffffffu, GA, 1);
+    if (lane < 31 && e < n_e) {
+      float inv = 0.f;
+      if (k >= 0 && k + 1 < nW) {
+        const float dl = lp_next - lp;
+        inv = dl > 0.f ? 1.f / dl : 0.f;
+      }
+      const float lpw = (k + 1 >= nW) ? kFltMax : lp_next;
+      row_a[e] = make_float4(lp, (G_next - G) * inv, G, lpw);
+      row_b[e] = make_float4(GZ, (GZ_next - GZ) * inv, GA, (GA_next - GA) * inv);
+    }
+  }
+}
+
+// The 8 partial sums of one particle over this thread's R wavelengths.
+template <int R, bool kGeneric>
+__device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
+                                         const float4* __restrict__ rb, int ks, int ke, float B,
+                                         float A0, const int2* __restrict__ s_bucket,
+                                         const float (&lam)[R], const float (&dlam)[R],
+                                         const float (&h)[R], const float (&hx)[R],
+                                         const float (&dx)[R], float (&s)[kAdjSums]) {
+  const float u = A0 - B;
+  int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
+  b = min(max(b, 0), kBuckets - 1);
+  const int2 te = s_bucket[b];
+  int k = te.x + (u >= __int_as_float(te.y) ? 1 : 0);
+  k = min(max(k, ks), ke);
+  float4 e = ra[k];
+  {
+    const float x = lam[0];
+    while (k > ks && x < e.x) { --k; e = ra[k]; }
+    while (k < ke && x >= e.w) { ++k; e = ra[k]; }
+  }
+  float4 f = rb[k];
+#pragma unroll
+  for (int i = 0; i < kAdjSums; ++i) s[i] = 0.f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float x = lam[r];
+    if (kGeneric) {
+      bool moved = false;
+      while (k < ke && x >= e.w) { ++k; e = ra[k]; moved = true; }
+      if (moved) f = rb[k];
+    } else if (r > 0 && x >= e.w) {
+      ++k;
+      e = ra[k];
+      f = rb[k];
+    }
+    const float d = x - e.x;
+    const float I = fmaf(d, e.y, e.z);
+    const float IZ = fmaf(d, f.y, f.x);
+    const float IA = fmaf(d, f.w, f.z);
+    s[0] = fmaf(h[r], I, s[0]);
+    s[1] = fmaf(dlam[r], I, s[1]);
+    s[2] = fmaf(h[r], IZ, s[2]);
+    s[3] = fmaf(dlam[r], IZ, s[3]);
+    s[4] = fmaf(h[r], IA, s[4]);
+    s[5] = fmaf(dlam[r], IA, s[5]);
+    s[6] = fmaf(hx[r], e.y, s[6]);
+    s[7] = fmaf(dx[r], e.y, s[7]);
+  }
+}
+
+// Sums 8 values over the warp with 9 shuffles (transposed butterfly).  Afterwards lane
+// l with (l & 3) == 0 holds the total of value ((l >> 4) & 1) * 4 + ((l >> 3) & 1) * 2 +
+// ((l >> 2) & 1).
+__device__ __forceinline__ float warp_reduce8(const float (&v)[8], int lane) {
+  float a[4];
+  const bool b4 = lane & 16;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float mine = b4 ? v[4 + i] : v[i];
+    const float other = b4 ? v[i] : v[4 + i];
+    a[i] = mine + __shfl_xor_sync(0xffffffffu, other, 16);
+  }
+  float c[2];
+  const bool b3 = lane & 8;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float mine = b3 ? a[2 + i] : a[i];
+    const float other = b3 ? a[i] : a[2 + i];
+    c[i] = mine + __shfl_xor_sync(0xffffffffu, other, 8);
+  }
+  const bool b2 = lane & 4;
+  float d = (b2 ? c[1] : c[0]) + __shfl_xor_sync(0xffffffffu, b2 ? c[0] : c[1], 4);
+  d += __shfl_xor_sync(0xffffffffu, d, 2);
+  d += __shfl_xor_sync(0xffffffffu, d, 1);
+  return d;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const AdjSmem SL = adj_smem_layout(a.n_wave, a.nZ + a.nA, a.row_cap);
+  float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
+  int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
+  float* s_grid = reinterpret_cast<float*>(smem + SL.grid);
+  float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);
+  float4* s_ra = reinterpret_cast<float4*>(smem + SL.row_a);
+  float4* s_rb = reinterpret_cast<float4*>(smem + SL.row_b);
+  float* s_red = reinterpret_cast<float*>(smem + SL.red);  // [2][warps][8]
+  ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);
+  __shared__ uint64_t s_bar;
+  __shared__ int s_item, s_fail;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < a.n_wave; i += kAdjThreads) s_wz[i] = a.wave_z[i];
+  for (int b = tid; b < kBuckets; b += kAdjThreads) s_bucket[b] = a.bucket[b];
+  for (int i = tid; i < a.nZ; i += kAdjThreads) s_grid[i] = a.zg[i];
+  for (int i = tid; i < a.nA; i += kAdjThreads) s_grid[a.nZ + i] = a.ag[i];
+  if (tid == 0) {
+    mbar_init(&s_bar, 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  const int n_t = a.n_t;
+  const int t0 = tid * R;
+  float lam[R], dlam[R], dx[R], h[R], hx[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int t = t0 + r;
+    const int tc = t < n_t ? t : n_t - 1;
+    lam[r] = a.wave_t[tc];
+    dlam[r] = (t < n_t && t > 0) ? (a.wave_t[t] - a.wave_t[t - 1]) : 0.f;
+    dx[r] = dlam[r] * lam[r];
+  }
+  const float A0 = a.At[t0 < n_t ? t0 : n_t - 1];
+  const int n_items = a.ctrl->n_items;
+  uint32_t phase = 0;
+  int step = 0;
+  __syncthreads();
+
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(&a.ctrl->next_item, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= n_items) break;
+    const int2 it = a.items[item];
+    const int s = it.x, chunk = it.y;
+    const int seg_b = a.seg_off[s], seg_e = a.seg_off[s + 1];
+    const long long jb = (long long)seg_b + (long long)chunk * kChunk;
+    const long long je = min((long long)seg_e, jb + kChunk);
+    const int np = (int)(je - jb);
+    const float* adj = a.adj + (long long)s * a.adj_stride;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      h[r] = (t0 + r < n_t) ? adj[t0 + r] : 0.f;
+      hx[r] = h[r] * lam[r];
+    }
+    for (int i = tid; i < np; i += kAdjThreads) s_rec[i] = a.rec[jb + i];
+    __syncthreads();
+    if (np > 0 && tid == 0) adj_issue(a, s_rec[0], s_stage, &s_bar);
+
+    for (int p = 0; p < np; ++p, ++step) {
+      const int buf = step & 1;
+      const ParticleRec& rec = s_rec[p];
+      if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
+      phase ^= 1u;
+      adj_build(a, rec, s_wz, s_grid, s_stage, s_ra, s_rb, lane, warp);
+      __syncthreads();  // rows ready; staging consumed
+      if (s_fail) {
+        if (tid == 0) {
+          atomicExch(&a.ctrl->error, 1);
+          mbar_wait_bounded(&s_bar, phase ^ 1u);
+        }
+        return;
+      }
+      if (p + 1 < np && tid == 0) adj_issue(a, s_rec[p + 1], s_stage, &s_bar);
+      const int4 rb = rec.b;
+      const int ks = rb.y, ke = rb.z & ~kGenericFlag;
+      float sums[kAdjSums];
+      if (rb.z & kGenericFlag)
+        adj_eval<R, true>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h, hx,
+                          dx, sums);
+      else
+        adj_eval<R, false>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h, hx,
+                           dx, sums);
+      const float wv = warp_reduce8(sums, lane);
+      if ((lane & 3) == 0) {
+        const int v = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+        s_red[(buf * kAdjWarps + warp) * kAdjSums + v] = wv;
+      }
+      __syncthreads();  // partial sums visible; rows free for the next particle
+      if (warp == 0) {
+        float tot = 0.f;
+        if (lane < kAdjSums)
+          for (int w = 0; w < kAdjWarps; ++w) tot += s_red[(buf * kAdjWarps + w) * kAdjSums + lane];
+        const float gamma = __shfl_sync(0xffffffffu, tot, 0);
+        const float Tp = __shfl_sync(0xffffffffu, tot, 1);
+        const float HZ = __shfl_sync(0xffffffffu, tot, 2);
+        const float DZ = __shfl_sync(0xffffffffu, tot, 3);
+        const float HA = __shfl_sync(0xffffffffu, tot, 4);
+        const float DA = __shfl_sync(0xffffffffu, tot, 5);
+        const float HV = __shfl_sync(0xffffffffu, tot, 6);
+        const float DV = __shfl_sync(0xffffffffu, tot, 7);
+        if (lane == 0) {
+          const float m = rec.a.x, T = rec.c.x, TZ = rec.c.y, TA = rec.c.z;
+          const float sc = T / Tp;
+          float gm = 0.f, gz = 0.f, ga = 0.f, gv = 0.f;
+          if (Tp != 0.f && isfinite(sc)) {
+            const float beta = m * sc;
+            const float k = m / Tp;
+            const float inv_c = (float)(1.0 / kSpeedOfLight);
+            gm = sc * gamma;
+            gz = fmaf(beta, HZ, gamma * k * (TZ - sc * DZ));
+            ga = fmaf(beta, HA, gamma * k * (TA - sc * DA));
+            // dI/dv = -lambda * slope / c, dT/dv = T / c
+            gv = fmaf(-beta * inv_c, HV, gamma * k * inv_c * (T + sc * DV));
+          }
+          const long long i = a.perm[jb + p];
+          if (a.g_mass) a.g_mass[i] = gm;
+          if (a.g_met) a.g_met[i] = gz;
+          if (a.g_age) a.g_age[i] = ga;
+          if (a.g_vlos) a.g_vlos[i] = gv;
+        }
+      }
+    }
+  }
+}
+
+template <int R>
+int launch_adjoint(const AdjArgs& args, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(cube_adjoint_kernel<R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess)
+    return set_error(RUBIX_E_CUDA, "cudaFuncSetAttribute(cube_adjoint_kernel): %s",
+                     cudaGetErrorString(e));
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_adjoint_kernel<R>, kAdjThreads,
+                                                    smem);
+  if (e != cudaSuccess || per_sm < 1)
+    return set_error(RUBIX_E_UNSUPPORTED,
+                     "cube_adjoint_kernel does not fit on an SM with %zu bytes of shared memory",
+                     smem);
+  cube_adjoint_kernel<R><<<sm_count() * per_sm, kAdjThreads, smem, st>>>(args);
+  RUBIX_LAUNCH_CHECK("cube_adjoint_kernel");
+  return RUBIX_OK;
+}
+
+}  // namespace
+}  // namespace rubix
+
+using namespace rubix;
+
+extern "C" size_t rubix_cube_bwd_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
+                                                int32_t n_met, int32_t n_age, int32_t n_wave) {
+  if (n < 0 || n_segments < 0 || n_wave_t < 0 || n_met < 0 || n_age < 0 || n_wave < 0) return 0;
+  return carve_cube(nullptr, n, n_segments, n_wave_t, n_met, n_age, n_wave).bytes;
+}
+
+extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicity,
+                              const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                              int32_t n_age, int32_t n_wave, const float* wave_t,
+                              int32_t n_wave_t, const float* mass, const float* metallicity,
+                              const float* age, const float* velocity, int64_t vel_stride,
+                              int32_t vel_component, const int32_t* perm,
+                              const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                              const float* adj, int64_t adj_stride, float* grad_mass,
+                              float* grad_metallicity, float* grad_age, float* grad_vlos,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "rubix_cube_bwd: bad n");
+  RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "rubix_cube_bwd: n_segments < 0");
+  RUBIX_REQUIRE(n_met >= 2 && n_age >= 2, RUBIX_E_SHAPE,
+                "rubix_cube_bwd: SSP grid needs >= 2 metallicities and >= 2 ages");
+  RUBIX_REQUIRE(n_wave >= 2, RUBIX_E_SHAPE, "rubix_cube_bwd: SSP grid needs >= 2 wavelengths");
+  RUBIX_REQUIRE(n_wave_t >= 1 && n_wave_t <= kMaxWaveT, RUBIX_E_SHAPE,
+                "rubix_cube_bwd: n_wave_t must be in [1, %d], got %d", kMaxWaveT, n_wave_t);
+  RUBIX_REQUIRE(adj_stride >= n_wave_t, RUBIX_E_SHAPE, "rubix_cube_bwd: adj_stride < n_wave_t");
+  RUBIX_REQUIRE(vel_component >= 0 && vel_component < vel_stride, RUBIX_E_INVALID,
+                "rubix_cube_bwd: vel_component outside the velocity row");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // every gradient entry is written: zeros for particles outside the sorted set
+  float* grads[4] = {grad_mass, grad_metallicity, grad_age, grad_vlos};
+  for (float* g : grads)
+    if (g && n > 0) RUBIX_CUDA_TRY(cudaMemsetAsync(g, 0, sizeof(float) * (size_t)n, st));
+  if (n_segments == 0 || n == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(ssp_flux && ssp_metallicity && ssp_age && ssp_wave_z && wave_t && seg_offsets &&
+                    adj && mass && metallicity && age && velocity && perm,
+                RUBIX_E_INVALID, "rubix_cube_bwd: null pointer");
+  const size_t need = rubix_cube_bwd_workspace_size(n, n_segments, n_wave_t, n_met, n_age, n_wave);
+  RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
+                "rubix_cube_bwd: workspace of %zu bytes needed, %zu given", need, workspace_bytes);
+  RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
+                "rubix_cube_bwd: workspace must be 256-byte aligned");
+  const int row_cap = n_wave + 2;
+  const AdjSmem SL = adj_smem_layout(n_wave, n_met + n_age, row_cap);
+  RUBIX_REQUIRE(SL.total <= 227 * 1024, RUBIX_E_UNSUPPORTED,
+                "rubix_cube_bwd: SSP grid of %d wavelengths needs %zu bytes of shared memory "
+                "(limit 232448)",
+                n_wave, SL.total);
+
+  const CubeLayout L = carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave);
+  const CubeInputs in{ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met, n_age, n_wave,
+                      wave_t, n_wave_t, mass, metallicity, age, velocity, vel_stride,
+                      vel_component, perm, seg_offsets, n_segments, n};
+  {
+    const int rc = cube_prepare(in, L, /*with_grad=*/true, st);
+    if (rc != RUBIX_OK) return rc;
+  }
+  AdjArgs args;
+  args.ct = L.ct;
+  args.wave_z = ssp_wave_z;
+  args.nZ = n_met;
+  args.nA = n_age;
+  args.n_wave = n_wave;
+  args.zg = ssp_metallicity;
+  args.ag = ssp_age;
+  args.wave_t = wave_t;
+  args.At = L.At;
+  args.n_t = n_wave_t;
+  args.rec = L.rec;
+  args.seg_off = seg_offsets;
+  args.perm = perm;
+  args.items = L.items;
+  args.adj = adj;
+  args.adj_stride = adj_stride;
+  args.g_mass = grad_mass;
+  args.g_met = grad_metallicity;
+  args.g_age = grad_age;
+  args.g_vlos = grad_vlos;
+  args.ctrl = L.ctrl;
+  args.bucket = L.bucket;
+  args.row_cap = row_cap;
+  const int need_r = (n_wave_t + kAdjThreads - 1) / kAdjThreads;
+  const size_t smem = SL.total;
+  if (need_r <= 1) return launch_adjoint<1>(args, smem, st);
+  if (need_r <= 2) return launch_adjoint<2>(args, smem, st);
+  if (need_r <= 4) return launch_adjoint<4>(args, smem, st);
+  if (need_r <= 8) return launch_adjoint<8>(args, smem, st);
+  if (need_r <= 12) return launch_adjoint<12>(args, smem, st);
+  if (need_r <= 15) return launch_adjoint<15>(args, smem, st);
+  return launch_adjoint<16>(args, smem, st);
+}

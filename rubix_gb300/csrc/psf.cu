@@ -89,18 +89,34 @@ __global__ void __launch_bounds__(kPsfThreads) psf_strip_kernel(PsfArgs a) {
 }
 
 
-// Register-blocked variant for equal odd-or-even tap counts M <= 25: each thread owns
-// one wavelength lane and kPsfXB consecutive x positions; the y window of the last M
+// Register-blocked variant for equal tap counts M <= 21: each thread owns one
+// wavelength lane and kPsfXB consecutive x positions; the y window of the last M
 // x-convolved rows lives in registers (the row loop is unrolled by M so every window
-// index is static) and the next input row is prefetched into registers while the
-// current one is convolved, so each row costs one barrier.
+// index is static).  Input rows are staged by 4-byte cp.async copies into a ring of
+// kPsfStages shared-memory rows, kPsfStages-1 rows ahead of the row being convolved,
+// so each SM keeps several rows of every strip in flight; one barrier per row.
 constexpr int kPsfXB = 4;
+constexpr int kPsfStages = 4;
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  const int n = valid ? 4 : 0;  // 0: zero-fill, nothing read
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 template <int M>
 __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
   constexpr int W = kPsfTileX + M - 1;  // staged row width
   constexpr int PER = (W * kPsfTileL + kPsfThreads - 1) / kPsfThreads;
-  __shared__ float s_in[2][W * kPsfTileL];
+  __shared__ float s_in[kPsfStages][W * kPsfTileL];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = blockIdx.x * kPsfTileX;
   const int l0 = blockIdx.y * kPsfTileL;
@@ -114,25 +130,32 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
     tx[i] = a.tx[i];
   }
   const int total = a.ny + a.oy;  // input rows 0 .. ny-1+oy
-  float pre[PER];
-  auto load_row = [&](int r) {
+  // This thread's copies of a staged row: element q = tid + k*256 (column jj = q / 32,
+  // lane ll = q % 32) comes from row_base + off[k]; the column/wavelength validity is
+  // the same for every row.
+  int off[PER];
+  unsigned valid = 0u;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int q = tid + k * kPsfThreads;
+    const int jj = q / kPsfTileL, ll = q % kPsfTileL;
+    const int xg = xsrc0 + jj, lg = l0 + ll;
+    const bool ok = q < W * kPsfTileL && xg >= 0 && xg < a.nx && lg < a.nl;
+    off[k] = ok ? (int)((long long)xg * a.sin + lg) : 0;
+    valid |= ok ? (1u << k) : 0u;
+  }
+  const long long row_stride = (long long)a.nx * a.sin;
+  auto issue_row = [&](int r) {
+    float* dst = s_in[r % kPsfStages];
+    const float* base = a.in + (long long)r * row_stride;
+    const bool row_ok = r < a.ny;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       const int q = tid + k * kPsfThreads;
-      float v = 0.f;
-      if (q < W * kPsfTileL && r < a.ny) {
-        const int jj = q / kPsfTileL, ll = q % kPsfTileL;
-        const int xg = xsrc0 + jj, lg = l0 + ll;
-        if (xg >= 0 && xg < a.nx && lg < a.nl) v = a.in[((long long)r * a.nx + xg) * a.sin + lg];
+      if (q < W * kPsfTileL) {
+        const bool ok = row_ok && ((valid >> k) & 1u);
+        cp_async4(dst + q, ok ? base + off[k] : a.in, ok);
       }
-      pre[k] = v;
-    }
-  };
-  auto store_row = [&](int buf) {
-#pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const int q = tid + k * kPsfThreads;
-      if (q < W * kPsfTileL) s_in[buf][q] = pre[k];
     }
   };
   float win[M][kPsfXB];
@@ -141,20 +164,28 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
 #pragma unroll
     for (int j = 0; j < kPsfXB; ++j) win[i][j] = 0.f;
 
-  load_row(0);
-  store_row(0);
-  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kPsfStages - 1; ++r) {
+    if (r < total) issue_row(r);
+    cp_async_commit();
+  }
   for (int r0 = 0; r0 < total; r0 += M) {
 #pragma unroll
     for (int jj = 0; jj < M; ++jj) {
       const int r = r0 + jj;
       if (r >= total) break;
-      const int buf = r & 1;
-      if (r + 1 < total) load_row(r + 1);
+      cp_async_wait<kPsfStages - 2>();  // row r has landed (this thread's copies)
+      __syncthreads();                   // ... and every thread's; row r-1 is consumed
+      {
+        const int rn = r + kPsfStages - 1;
+        if (rn < total) issue_row(rn);
+        cp_async_commit();
+      }
+      const float* row = s_in[r % kPsfStages];
       // x-pass over the staged row r for this thread's kPsfXB positions
       float xv[kPsfXB + M - 1];
 #pragma unroll
-      for (int q = 0; q < kPsfXB + M - 1; ++q) xv[q] = s_in[buf][(xb + q) * kPsfTileL + lane];
+      for (int q = 0; q < kPsfXB + M - 1; ++q) xv[q] = row[(xb + q) * kPsfTileL + lane];
 #pragma unroll
       for (int j = 0; j < kPsfXB; ++j) {
         float h = 0.f;
@@ -174,10 +205,9 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
           if (x < a.nx) a.out[((long long)y * a.nx + x) * a.sout + l] = o;
         }
       }
-      if (r + 1 < total) store_row(buf ^ 1);
-      __syncthreads();
     }
   }
+  cp_async_wait<0>();
 }
 
 template <int M>
@@ -223,7 +253,9 @@ extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx
     a.tx[i] = i < m_x ? tx[i] : 0.f;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (m_x == m_y) {
+  // the register kernel keeps per-row element offsets in 32 bits
+  const bool small_rows = (long long)nx * spaxel_stride_in < (1LL << 31);
+  if (m_x == m_y && small_rows) {
     switch (m_x) {
       case 1: return launch_psf_reg<1>(a, st);
       case 3: return launch_psf_reg<3>(a, st);

@@ -21,6 +21,8 @@ __all__ = [
     "cube_forward",
     "psf_forward",
     "lsf_forward",
+    "cube_backward",
+    "dot",
     "workspace",
 ]
 
@@ -165,6 +167,62 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
 
         err = ctypes.c_int(0)
         _lib.call("rubix_cube_status", _ptr(ws), ctypes.byref(err), _stream(dev))
+    return out
+
+
+def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, metallicity,
+                  age, velocity, vel_component, perm, seg_offsets, n_segments, adj):
+    """Gradients (mass, metallicity, age, v_los) of <adj, cube> with cube the output of
+    ``cube_forward`` without LSF; ``adj`` is [n_segments, >=L].  Four [n] tensors, zero
+    for particles outside the sorted set."""
+    ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
+    nz, na, nw = ssp_flux.shape
+    ssp_metallicity = _contig("ssp_metallicity", ssp_metallicity, torch.float32)
+    ssp_age = _contig("ssp_age", ssp_age, torch.float32)
+    ssp_wave_z = _contig("ssp_wave_z", ssp_wave_z, torch.float32)
+    wave_t = _contig("wave_t", wave_t, torch.float32)
+    mass = _contig("mass", mass, torch.float32).reshape(-1)
+    metallicity = _contig("metallicity", metallicity, torch.float32).reshape(-1)
+    age = _contig("age", age, torch.float32).reshape(-1)
+    velocity = _contig("velocity", velocity, torch.float32)
+    n = mass.numel()
+    if metallicity.numel() != n or age.numel() != n or velocity.shape[0] != n:
+        raise ValueError("particle arrays must all have the same length")
+    vstride = velocity.shape[1] if velocity.dim() == 2 else 1
+    perm = _contig("perm", perm, torch.int32)
+    seg_offsets = _contig("seg_offsets", seg_offsets, torch.int32)
+    L = wave_t.numel()
+    _check_cuda("adj", adj, torch.float32)
+    if adj.dim() != 2 or adj.shape[0] != n_segments or adj.shape[1] < L or adj.stride(1) != 1:
+        adj = adj.reshape(int(n_segments), -1).contiguous()
+    dev = mass.device
+    grads = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(4)]
+    nbytes = _lib.query("rubix_cube_bwd_workspace_size", n, int(n_segments), L, nz, na, nw)
+    ws = workspace(nbytes, dev)
+    _lib.call("rubix_cube_bwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
+              _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
+              _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
+              _ptr(seg_offsets), int(n_segments), n, _ptr(adj), adj.stride(0),
+              *[_ptr(g) for g in grads], _ptr(ws), ws.numel(), _stream(dev))
+    # setup, corner table, prefix, count, three scans, fill, adjoint (+ gather when n > 0)
+    _count((9 + (1 if n > 0 else 0)) if (n_segments > 0 and n > 0) else 0)
+    return tuple(grads)
+
+
+def dot(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """Deterministic sum(a * b) of two float32 CUDA tensors of equal size, as a 0-d
+    float64 tensor on the device."""
+    _check_cuda("a", a, torch.float32)
+    _check_cuda("b", b, torch.float32)
+    if a.numel() != b.numel():
+        raise ValueError("dot: sizes differ")
+    a = a.contiguous().reshape(-1)
+    b = b.contiguous().reshape(-1)
+    out = torch.empty((), dtype=torch.float64, device=a.device)
+    ws = workspace(_lib.query("rubix_dot_workspace_size"), a.device)
+    _lib.call("rubix_dot", _ptr(a), _ptr(b), a.numel(), _ptr(out), _ptr(ws), ws.numel(),
+              _stream(a.device))
+    _count(1)
     return out
 
 
