@@ -11,15 +11,15 @@
 //     kstart/kend of both ends of the telescope range on the particle's float32 grid
 //     lambda'_k = fl32(lambda_z,k * alpha)).
 //   * Work items are (spaxel, chunk of <= kChunk particles), largest first, pulled by a
-//     persistent kernel from an atomic counter.  A block of 256 threads owns the
+//     persistent kernel from an atomic counter.  A block of 384 threads owns the
 //     telescope grid of its spaxel: thread i holds R consecutive wavelengths
 //     t = i*R + r in registers (wavelength, bin width, accumulator).
-//   * Per batch of kPB particles one thread issues a 1-D TMA bulk copy of each
-//     particle's corner-table segment (its bracket range only) into shared memory; it
-//     completes on an mbarrier while the block evaluates the previous batch.  The block
-//     then builds per particle the row of entries (lambda'_k, slope_k, G_k,
-//     lambda'_{k+1}) of the mixed template G = sum_c w_c F_c and the in-range flux sum T
-//     (rubix/spectra/ifu.py:241-245).
+//   * Per batch of kPB particles the block builds, per particle, the row of entries
+//     (lambda'_k, slope_k, G_k, lambda'_{k+1}) of the mixed template G = sum_c w_c F_c
+//     over the particle's bracket range, reading the corners from the L2-resident corner
+//     table.  Rows are double-buffered: while the block evaluates batch b it builds
+//     batch b+1, so each batch costs one barrier.  The in-range flux sum T
+//     (rubix/spectra/ifu.py:241-245) comes from the gather (prefix sums).
 //   * Evaluation: each thread finds the exact bracket of its first wavelength (bucket
 //     table + exact comparisons on lambda') and walks forward over its R wavelengths;
 //     when every SSP interval is wider than every telescope bin the walk advances at
@@ -32,7 +32,6 @@
 //   * Optional epilogue: the LSF convolution along wavelength of the finished spectrum
 //     (rubix/telescope/lsf/lsf.py:29-105), which commutes with the PSF.
 #include "cube_common.cuh"
-#include "tma.cuh"
 
 namespace rubix {
 namespace {
@@ -59,9 +58,10 @@ struct MainArgs {
   float lsf[kMaxLsfTaps + 1];
 };
 
-// Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned).
+// Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned).  The rows
+// are double-buffered: [2][kPB][row_cap] entries.
 struct SmemLayout {
-  size_t wz, bucket, stage, rows, red, rec, total;
+  size_t wz, bucket, rows, red, rec, total;
 };
 
 __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
@@ -70,9 +70,8 @@ __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
   auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
   L.wz = o;     o = al(o + sizeof(float) * n_wave);
   L.bucket = o; o = al(o + sizeof(int2) * kBuckets);
-  L.stage = o;  o = al(o + sizeof(float4) * kPB * (size_t)row_cap);
   L.rows = o;   // also holds the zero-padded spectrum of the LSF epilogue
-  o = al(o + std::max(sizeof(float4) * kPB * (size_t)row_cap,
+  o = al(o + std::max(sizeof(float4) * 2 * kPB * (size_t)row_cap,
                       sizeof(float) * (size_t)(kMaxWaveT + 2 * kMaxLsfTaps + 8)));
   L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 2);
   L.rec = o;    o = al(o + sizeof(ParticleRec) * kChunk);
@@ -80,45 +79,16 @@ __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
   return L;
 }
 
-// Thread 0: arm the barrier and issue one bulk copy per particle of the batch: the
-// corner-table entries k in [max(kstart,0), min(kend+1, nW-1)] of its cell.
-__device__ __forceinline__ void issue_stage(const MainArgs& a, const ParticleRec* recs, int cnt,
-                                            float4* stage, uint64_t* bar) {
-  fence_proxy_async_smem();  // earlier generic reads of the staging buffer come first
-  uint32_t bytes = 0;
-  int klo[kPB], nk[kPB], cells[kPB];
-#pragma unroll
-  for (int p = 0; p < kPB; ++p) {
-    cells[p] = -1;
-    klo[p] = 0;
-    nk[p] = 0;
-    if (p < cnt) {
-      const int4 b = recs[p].b;
-      const int ks = b.y, ke = b.z & ~kGenericFlag;
-      klo[p] = max(ks, 0);
-      nk[p] = min(ke + 1, a.n_wave - 1) - klo[p] + 1;
-      cells[p] = b.x;
-      if (b.x >= 0) bytes += 16u * (uint32_t)nk[p];
-    }
-  }
-  mbar_arrive_expect_tx(bar, bytes);
-#pragma unroll
-  for (int p = 0; p < kPB; ++p)
-    if (cells[p] >= 0)
-      bulk_copy_g2s(stage + (size_t)p * a.row_cap, a.ct + (long long)cells[p] * a.n_wave + klo[p],
-                    16u * nk[p], bar);
-}
-
 struct RowParams {
   float alpha, w00, w10, w01, w11;
   int ks, klo, khi, n_e;
   bool has_cell;
-  const float4* st;  // st[k] = staged corners of SSP wavelength k
+  const float4* ct;  // ct[k] = corners of SSP wavelength k of the particle's cell (global)
   float4* row;
 };
 
-__device__ __forceinline__ RowParams row_params(const ParticleRec& r, int nW,
-                                                const float4* stage, float4* row) {
+__device__ __forceinline__ RowParams row_params(const ParticleRec& r, const MainArgs& a,
+                                                float4* row) {
   RowParams q;
   const float tz = r.a.w, ta = __int_as_float(r.b.w);
   const int ke = r.b.z & ~kGenericFlag;
@@ -129,10 +99,10 @@ __device__ __forceinline__ RowParams row_params(const ParticleRec& r, int nW,
   q.w11 = tz * ta;
   q.ks = r.b.y;
   q.klo = max(q.ks, 0);
-  q.khi = min(ke + 1, nW - 1);
+  q.khi = min(ke + 1, a.n_wave - 1);
   q.n_e = ke - q.ks + 1;
   q.has_cell = r.b.x >= 0;
-  q.st = stage - q.klo;
+  q.ct = a.ct + (long long)(q.has_cell ? r.b.x : 0) * a.n_wave;
   q.row = row;
   return q;
 }
@@ -140,16 +110,16 @@ __device__ __forceinline__ RowParams row_params(const ParticleRec& r, int nW,
 // One warp step of a row build: entries base .. base+30 (lane 31 supplies the right
 // neighbour).  Entry e (SSP index k = kstart + e) = (lambda'_k, slope_k, G_k,
 // lambda'_{k+1}), with sentinels (-FLT_MAX, 0, G_0, lambda'_0) for k = -1 and
-// slope 0 / FLT_MAX beyond the grid.
+// slope 0 / FLT_MAX beyond the grid.  The corners come from the L2-resident table.
 __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
                                            const float* __restrict__ s_wz, int lane) {
   const int e = base + lane;
   const int k = q.ks + e;
   if (q.ks + base >= 0 && q.ks + base + 31 <= q.khi) {
-    // interior step: every lane, neighbour included, is a staged SSP wavelength
+    // interior step: every lane, neighbour included, is an SSP wavelength of the range
     float G = 0.f;
     if (q.has_cell) {
-      const float4 c = q.st[k];
+      const float4 c = __ldg(q.ct + k);
       G = q.w00 * c.x;
       G = fmaf(q.w10, c.y, G);
       G = fmaf(q.w01, c.z, G);
@@ -167,7 +137,7 @@ __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
     const int kk = min(max(k, q.klo), q.khi);
     float G = 0.f;
     if (q.has_cell) {
-      const float4 c = q.st[kk];
+      const float4 c = __ldg(q.ct + kk);
       G = q.w00 * c.x;
       G = fmaf(q.w10, c.y, G);
       G = fmaf(q.w01, c.z, G);
@@ -188,14 +158,14 @@ __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
   }
 }
 
-// Builds the rows of the (one or two) particles of a batch, interleaving their steps.
+// Builds the rows of the (one or two) particles of a batch into `rows`
+// ([kPB][row_cap]), interleaving their steps.
 __device__ __forceinline__ void build_rows(const MainArgs& a, const ParticleRec* recs, int cnt,
                                            const float* __restrict__ s_wz,
-                                           const float4* __restrict__ stage,
                                            float4* __restrict__ rows, int lane, int warp) {
-  const RowParams q0 = row_params(recs[0], a.n_wave, stage, rows);
+  const RowParams q0 = row_params(recs[0], a, rows);
   if (cnt > 1) {
-    const RowParams q1 = row_params(recs[1], a.n_wave, stage + a.row_cap, rows + a.row_cap);
+    const RowParams q1 = row_params(recs[1], a, rows + a.row_cap);
     const int n_max = max(q0.n_e, q1.n_e);
     for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
       if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
@@ -220,6 +190,23 @@ __device__ __forceinline__ float warp_reduce2(float v0, float v1, int lane) {
   return c;
 }
 
+// Bracket of this thread's first wavelength on a particle's row: bucket table in log
+// wavelength, then exact comparisons on lambda'.
+__device__ __forceinline__ int first_bracket(const float4* __restrict__ rowp, int ks, int ke,
+                                             float B, float A0, const int2* __restrict__ s_bucket,
+                                             float x0, float4& e) {
+  const float u = A0 - B;
+  int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
+  b = min(max(b, 0), kBuckets - 1);
+  const int2 te = s_bucket[b];
+  int k = te.x + (u >= __int_as_float(te.y) ? 1 : 0);
+  k = min(max(k, ks), ke);
+  e = rowp[k];
+  while (k > ks && x0 < e.x) { --k; e = rowp[k]; }
+  while (k < ke && x0 >= e.w) { ++k; e = rowp[k]; }
+  return k;
+}
+
 // Interpolated values of one particle at this thread's R wavelengths; returns the
 // partial sum of I_t * dlambda_t.
 template <int R, bool kGeneric>
@@ -228,18 +215,8 @@ __device__ __forceinline__ float eval_particle(const float4* __restrict__ rowp, 
                                                const int2* __restrict__ s_bucket,
                                                const float (&lam)[R], const float (&dlam)[R],
                                                float (&I)[R]) {
-  const float u = A0 - B;
-  int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
-  b = min(max(b, 0), kBuckets - 1);
-  const int2 te = s_bucket[b];
-  int k = te.x + (u >= __int_as_float(te.y) ? 1 : 0);
-  k = min(max(k, ks), ke);
-  float4 e = rowp[k];
-  {
-    const float x = lam[0];
-    while (k > ks && x < e.x) { --k; e = rowp[k]; }
-    while (k < ke && x >= e.w) { ++k; e = rowp[k]; }
-  }
+  float4 e;
+  int k = first_bracket(rowp, ks, ke, B, A0, s_bucket, lam[0], e);
   float tp = 0.f;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -255,6 +232,43 @@ __device__ __forceinline__ float eval_particle(const float4* __restrict__ rowp, 
     tp = fmaf(v, dlam[r], tp);
   }
   return tp;
+}
+
+// Both particles of a batch on the one-step walk, interleaved for instruction-level
+// parallelism (their shared-memory loads and FMA chains overlap).
+template <int R>
+__device__ __forceinline__ void eval_pair(const float4* __restrict__ row0, int ks0, int ke0,
+                                          float B0, const float4* __restrict__ row1, int ks1,
+                                          int ke1, float B1, float A0,
+                                          const int2* __restrict__ s_bucket,
+                                          const float (&lam)[R], const float (&dlam)[R],
+                                          float (&I0)[R], float (&I1)[R], float& tp0,
+                                          float& tp1) {
+  float4 e0, e1;
+  int k0 = first_bracket(row0, ks0, ke0, B0, A0, s_bucket, lam[0], e0);
+  int k1 = first_bracket(row1, ks1, ke1, B1, A0, s_bucket, lam[0], e1);
+  tp0 = 0.f;
+  tp1 = 0.f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float x = lam[r];
+    if (r > 0) {
+      if (x >= e0.w) {
+        ++k0;
+        e0 = row0[k0];
+      }
+      if (x >= e1.w) {
+        ++k1;
+        e1 = row1[k1];
+      }
+    }
+    const float v0 = fmaf(x - e0.x, e0.y, e0.z);
+    const float v1 = fmaf(x - e1.x, e1.y, e1.z);
+    I0[r] = v0;
+    I1[r] = v1;
+    tp0 = fmaf(v0, dlam[r], tp0);
+    tp1 = fmaf(v1, dlam[r], tp1);
+  }
 }
 
 // LSF along wavelength of one spectrum: s_pad holds the spectrum at offset
@@ -279,25 +293,19 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   const SmemLayout SL = smem_layout(a.n_wave, a.row_cap);
   float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
   int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
-  float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);
-  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);
+  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);        // [2][kPB][row_cap]
   float* s_red = reinterpret_cast<float*>(smem + SL.red);            // [2][warps][2]
   ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);  // records of the item
   float* s_spec = reinterpret_cast<float*>(s_rows);  // LSF epilogue reuses the rows
-  __shared__ uint64_t s_bar;
-  __shared__ int s_item, s_last, s_fail;
+  __shared__ int s_item, s_last;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < a.n_wave; i += kAccThreads) s_wz[i] = a.wave_z[i];
   for (int b = tid; b < kBuckets; b += kAccThreads) s_bucket[b] = a.bucket[b];
-  if (tid == 0) {
-    mbar_init(&s_bar, 1);
-    fence_mbar_init();
-    s_fail = 0;
-  }
 
   const int n_t = a.n_t;
   const int t0 = tid * R;
+  const size_t buf_stride = (size_t)kPB * a.row_cap;
   float lam[R], dlam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -308,7 +316,6 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   }
   const float A0 = a.At[t0 < n_t ? t0 : n_t - 1];
   const int n_items = a.ctrl->n_items;
-  uint32_t phase = 0;
   __syncthreads();
 
   for (;;) {
@@ -328,60 +335,69 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = 0.f;
     // records of this item into shared memory (one 48-byte record per thread)
-    for (int i = tid; i < np; i += kAccThreads) {
-      const ParticleRec rr = a.rec[jb + i];
-      s_rec[i] = rr;
-    }
+    for (int i = tid; i < np; i += kAccThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
-    if (nbatch > 0 && tid == 0) issue_stage(a, s_rec, min(kPB, np), s_stage, &s_bar);
+    if (nbatch > 0) build_rows(a, s_rec, min(kPB, np), s_wz, s_rows, lane, warp);
+    __syncthreads();  // rows of batch 0 ready
 
+    // Batch bt: build batch bt+1 into the other buffer, evaluate batch bt, one barrier.
     for (int bt = 0; bt < nbatch; ++bt) {
       const int buf = bt & 1;
       const int cnt = min(kPB, np - bt * kPB);
       const ParticleRec* recs = s_rec + bt * kPB;
-      if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
-      phase ^= 1u;
-      build_rows(a, recs, cnt, s_wz, s_stage, s_rows, lane, warp);
-      __syncthreads();  // rows ready; staging consumed
-      if (s_fail) {
-        if (tid == 0) {
-          atomicExch(&a.ctrl->error, 1);
-          mbar_wait_bounded(&s_bar, phase ^ 1u);  // give copies in flight a last chance
-        }
-        return;
-      }
-      if (bt + 1 < nbatch && tid == 0)
-        issue_stage(a, recs + kPB, min(kPB, np - (bt + 1) * kPB), s_stage, &s_bar);
+      if (bt + 1 < nbatch)
+        build_rows(a, recs + kPB, min(kPB, np - (bt + 1) * kPB), s_wz,
+                   s_rows + (buf ^ 1) * buf_stride, lane, warp);
+      const float4* rows = s_rows + buf * buf_stride;
       float I[kPB][R];
       float tp[kPB];
-#pragma unroll
-      for (int p = 0; p < kPB; ++p) {
-        tp[p] = 0.f;
-        if (p < cnt) {
-          const float B = recs[p].a.z;
-          const int4 rb = recs[p].b;
-          const int ks = rb.y, ke = rb.z & ~kGenericFlag;
-          const float4* rowp = s_rows + p * a.row_cap - ks;
-          tp[p] = (rb.z & kGenericFlag)
-                      ? eval_particle<R, true>(rowp, ks, ke, B, A0, s_bucket, lam, dlam, I[p])
-                      : eval_particle<R, false>(rowp, ks, ke, B, A0, s_bucket, lam, dlam, I[p]);
+      const float B0 = recs[0].a.z;
+      const int4 rb0 = recs[0].b;
+      const int ks0 = rb0.y, ke0 = rb0.z & ~kGenericFlag;
+      if (cnt > 1) {
+        const float B1 = recs[1].a.z;
+        const int4 rb1 = recs[1].b;
+        const int ks1 = rb1.y, ke1 = rb1.z & ~kGenericFlag;
+        if (!((rb0.z | rb1.z) & kGenericFlag)) {
+          eval_pair<R>(rows - ks0, ks0, ke0, B0, rows + a.row_cap - ks1, ks1, ke1, B1, A0,
+                       s_bucket, lam, dlam, I[0], I[1], tp[0], tp[1]);
         } else {
-#pragma unroll
-          for (int r = 0; r < R; ++r) I[p][r] = 0.f;
+          tp[0] = (rb0.z & kGenericFlag)
+                      ? eval_particle<R, true>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam, dlam,
+                                               I[0])
+                      : eval_particle<R, false>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam,
+                                                dlam, I[0]);
+          tp[1] = (rb1.z & kGenericFlag)
+                      ? eval_particle<R, true>(rows + a.row_cap - ks1, ks1, ke1, B1, A0,
+                                               s_bucket, lam, dlam, I[1])
+                      : eval_particle<R, false>(rows + a.row_cap - ks1, ks1, ke1, B1, A0,
+                                                s_bucket, lam, dlam, I[1]);
         }
+      } else {
+        tp[0] = (rb0.z & kGenericFlag)
+                    ? eval_particle<R, true>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam, dlam,
+                                             I[0])
+                    : eval_particle<R, false>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam, dlam,
+                                              I[0]);
+        tp[1] = 0.f;
+#pragma unroll
+        for (int r = 0; r < R; ++r) I[1][r] = 0.f;
       }
       // T'0, T'1 over the warp, then over the block (fixed order: deterministic).
       const float wsum = warp_reduce2(tp[0], tp[1], lane);
       if ((lane & 15) == 0) s_red[(buf * kAccWarps + warp) * 2 + (lane >> 4)] = wsum;
-      __syncthreads();
-      float v = (lane < 16) ? s_red[(buf * kAccWarps + (lane & 7)) * 2 + (lane >> 3)] : 0.f;
+      __syncthreads();  // partial sums of batch bt and rows of batch bt+1 ready
+      // lanes 0..15 take warp (lane & 15)'s partial of T'0, lanes 16..31 of T'1
+      const int wl = lane & 15;
+      float v = (wl < kAccWarps) ? s_red[(buf * kAccWarps + wl) * 2 + (lane >> 4)] : 0.f;
+      v += __shfl_xor_sync(0xffffffffu, v, 8);
       v += __shfl_xor_sync(0xffffffffu, v, 4);
       v += __shfl_xor_sync(0xffffffffu, v, 2);
       v += __shfl_xor_sync(0xffffffffu, v, 1);
-      // lane 0: T'0, lane 8: T'1
+      // lane 0: T'0, lane 16: T'1
       float beta_l = 0.f;
-      if (lane == 0 || lane == 8) {
-        const int p = lane >> 3;
+      if (lane == 0 || lane == 16) {
+        const int p = lane >> 4;
         const float4 ra = recs[p].a, rc = recs[p].c;  // lane-dependent index: shared memory
         float sc = rc.x / v;
         if (sc != sc) sc = 0.f;
@@ -390,7 +406,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
         beta_l = (p < cnt && m != 0.f) ? m * sc : 0.f;
       }
       const float beta0 = __shfl_sync(0xffffffffu, beta_l, 0);
-      const float beta1 = __shfl_sync(0xffffffffu, beta_l, 8);
+      const float beta1 = __shfl_sync(0xffffffffu, beta_l, 16);
 #pragma unroll
       for (int r = 0; r < R; ++r) acc[r] += fmaf(beta1, I[1][r], beta0 * I[0][r]);
     }
@@ -562,10 +578,10 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
   if (need_r <= 1) return launch_main<1>(args, smem, st);
   if (need_r <= 2) return launch_main<2>(args, smem, st);
   if (need_r <= 4) return launch_main<4>(args, smem, st);
+  if (need_r <= 6) return launch_main<6>(args, smem, st);
   if (need_r <= 8) return launch_main<8>(args, smem, st);
-  if (need_r <= 12) return launch_main<12>(args, smem, st);
-  if (need_r <= 15) return launch_main<15>(args, smem, st);
-  return launch_main<16>(args, smem, st);
+  if (need_r <= 10) return launch_main<10>(args, smem, st);
+  return launch_main<11>(args, smem, st);  // kAccThreads * 11 >= kMaxWaveT
 }
 
 extern "C" int rubix_cube_status(const void* workspace, int* device_error, void* stream) {

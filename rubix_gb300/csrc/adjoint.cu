@@ -25,7 +25,7 @@
 namespace rubix {
 namespace {
 
-constexpr int kAdjThreads = kAccThreads;
+constexpr int kAdjThreads = 256;
 constexpr int kAdjWarps = kAdjThreads / 32;
 constexpr int kAdjSums = 8;
 

@@ -11,15 +11,14 @@
 namespace rubix {
 namespace {
 
-constexpr int kAccThreads = 256;
+constexpr int kAccThreads = 384;  // forward kernel: 2 blocks of 12 warps per SM
 constexpr int kAccWarps = kAccThreads / 32;
 constexpr int kPB = 2;          // particles per batch (the block reduction packs 2x2 values)
 constexpr int kChunk = 256;     // particles per work item
 constexpr int kBigItem = 64;    // single-chunk spaxels with at least this many go first
 constexpr int kBuckets = 1024;  // log-wavelength bucket table entries
 constexpr double kVmaxKms = 10000.0;  // bucket table and one-step-walk check sized for this
-constexpr int kMaxR = 16;
-constexpr int kMaxWaveT = kAccThreads * kMaxR;
+constexpr int kMaxWaveT = 4096;  // telescope wavelengths per spectrum
 constexpr int kGenericFlag = 1 << 30;  // in rec.b.z: particle needs the general walk
 constexpr int kMaxLsfTaps = 63;
 
