@@ -295,6 +295,73 @@ RUBIX_API size_t rubix_dot_workspace_size(void);
 RUBIX_API int rubix_dot(const float* a, const float* b, int64_t n, double* out, void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Ragged batches of galaxies                                                */
+/* ------------------------------------------------------------------------- */
+/*
+ * No counterpart in rubix (rubix renders one galaxy per pipeline run,
+ * rubix/core/pipeline.py:137-170).  A batch of n_gal galaxies shares the SSP grid and
+ * the telescope wavelength grid; galaxy g owns particles [particle_offsets[g],
+ * particle_offsets[g+1]) and the square S_g x S_g spaxel grid stored as global spaxels
+ * [seg_base[g], seg_base[g] + S_g^2) of one concatenated cube.  All table arguments
+ * are DEVICE arrays.  With global spaxel ids the ordinary rubix_spaxel_sort,
+ * rubix_cube_fwd / rubix_cube_bwd (n_segments = seg_base[n_gal]) and rubix_lsf_fwd
+ * process the whole batch in one launch each.
+ */
+
+/*
+ * Per particle: spaxel assignment with its galaxy's ascending bin edges
+ * (edges[edge_offsets[g] .. edge_offsets[g+1])), as rubix_spaxel_assign; keep_out = 1
+ * when inside the galaxy's aperture [edges[0], edges[-1]] (as rubix_aperture_mask)
+ * and when the flat id is below S_g^2; idx_out = seg_base[g] + flat id (0 when not
+ * kept).
+ */
+RUBIX_API int rubix_ragged_assign(const float* coords, int64_t n, int64_t coord_stride,
+                                  const int64_t* particle_offsets, int32_t n_gal,
+                                  const float* edges, const int32_t* edge_offsets,
+                                  const int32_t* sbin, const int64_t* seg_base, int32_t* idx_out,
+                                  uint8_t* keep_out, void* stream);
+
+/*
+ * rubix_psf_fwd for every galaxy of a batch in one launch.  taps [n_gal][2][m]: the
+ * y and x taps of each galaxy zero-padded and centred to the odd size m <= 21.
+ * block_offsets[g] = sum over g' < g of ceil(S_g'/32) * ceil(n_wave_t/32) and
+ * n_blocks = block_offsets[n_gal] (host copy).
+ */
+RUBIX_API int rubix_ragged_psf_fwd(const float* in, float* out, int32_t n_wave_t,
+                                   int64_t spaxel_stride_in, int64_t spaxel_stride_out,
+                                   int32_t n_gal, const int32_t* sbin, const int64_t* seg_base,
+                                   const int32_t* block_offsets, int32_t n_blocks,
+                                   const float* taps, int32_t m, void* stream);
+
+/*
+ * out[g] (device doubles) = sum over i in [offsets[g], offsets[g+1]) of a[i] * b[i];
+ * deterministic (fixed split and order).  n_seg <= 65535.
+ */
+RUBIX_API size_t rubix_segmented_dot_workspace_size(int32_t n_seg);
+RUBIX_API int rubix_segmented_dot(const float* a, const float* b, const int64_t* offsets,
+                                  int32_t n_seg, double* out, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Tuning                                                                    */
+/* ------------------------------------------------------------------------- */
+/*
+ * No counterpart in rubix.  Work-item shape of rubix_cube_fwd / rubix_cube_bwd on a
+ * device: spaxels are processed in chunks of `chunk` particles (multiple of 32 in
+ * [32, 256]; default 256) and single-chunk spaxels with at least `big_item` particles
+ * are scheduled first (default 64).  Results do not depend on big_item; they depend
+ * on chunk only through the summation order of spaxels longer than one chunk.
+ * Workspace sizes follow the tuning current at query time.  A per-device table
+ * guarded by a mutex; set_(device, NULL) restores the defaults.
+ */
+typedef struct {
+  int32_t chunk;
+  int32_t big_item;
+} rubix_cube_tuning;
+RUBIX_API int rubix_cube_tuning_set(int32_t device, const rubix_cube_tuning* tuning);
+RUBIX_API int rubix_cube_tuning_get(int32_t device, rubix_cube_tuning* tuning);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,14 @@ SIGNATURES = {
          _vp, _i64, _vp, _vp, _vp, _vp,
          _vp, _sz, _vp],
     ),
+    "rubix_ragged_assign": (_c.c_int, [_vp, _i64, _i64, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
+                                       _vp, _vp]),
+    "rubix_ragged_psf_fwd": (_c.c_int, [_vp, _vp, _i32, _i64, _i64, _i32, _vp, _vp, _vp, _i32,
+                                        _vp, _i32, _vp]),
+    "rubix_segmented_dot_workspace_size": (_sz, [_i32]),
+    "rubix_segmented_dot": (_c.c_int, [_vp, _vp, _vp, _i32, _vp, _vp, _sz, _vp]),
+    "rubix_cube_tuning_set": (_c.c_int, [_i32, _vp]),
+    "rubix_cube_tuning_get": (_c.c_int, [_i32, _vp]),
     "rubix_dot_workspace_size": (_sz, []),
     "rubix_dot": (_c.c_int, [_vp, _vp, _i64, _vp, _vp, _sz, _vp]),
 }

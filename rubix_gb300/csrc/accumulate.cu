@@ -10,7 +10,7 @@
 //     alpha = fl32(exp(v/c)), cell and bilinear weights, and the SSP brackets
 //     kstart/kend of both ends of the telescope range on the particle's float32 grid
 //     lambda'_k = fl32(lambda_z,k * alpha)).
-//   * Work items are (spaxel, chunk of <= kChunk particles), largest first, pulled by a
+//   * Work items are (spaxel, chunk of <= `chunk` particles), largest first, pulled by a
 //     persistent kernel from an atomic counter.  A block of 384 threads owns the
 //     telescope grid of its spaxel: thread i holds R consecutive wavelengths
 //     t = i*R + r in registers (wavelength, bin width, accumulator).
@@ -26,7 +26,7 @@
 //     most once per wavelength (one predicated load).  Interpolated values stay in
 //     registers while T' = sum_t I_t dlambda_t is reduced over the block; then
 //     s = nan_to_num(T/T') and the accumulators take mass * s * I.
-//   * Spaxels with more than kChunk particles are split; each chunk writes a partial
+//   * Spaxels with more than `chunk` particles are split; each chunk writes a partial
 //     spectrum to the workspace and the last chunk to finish sums the partials in chunk
 //     order (Kahan).  No float atomics: results are bit-reproducible.
 //   * Optional epilogue: the LSF convolution along wavelength of the finished spectrum
@@ -54,6 +54,7 @@ struct MainArgs {
   CubeCtrl* ctrl;
   const int2* bucket;
   int row_cap;
+  int chunk;            // particles per work item
   int lsf_k, lsf_crop;  // lsf_k = 0: no LSF epilogue
   float lsf[kMaxLsfTaps + 1];
 };
@@ -74,7 +75,7 @@ __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
   o = al(o + std::max(sizeof(float4) * 2 * kPB * (size_t)row_cap,
                       sizeof(float) * (size_t)(kMaxWaveT + 2 * kMaxLsfTaps + 8)));
   L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 2);
-  L.rec = o;    o = al(o + sizeof(ParticleRec) * kChunk);
+  L.rec = o;    o = al(o + sizeof(ParticleRec) * kMaxChunk);
   L.total = o;
   return L;
 }
@@ -327,8 +328,8 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
     const int s = it.x, chunk = it.y;
     const int seg_b = a.seg_off[s], seg_e = a.seg_off[s + 1];
     const int cnt_s = seg_e - seg_b;
-    const long long jb = (long long)seg_b + (long long)chunk * kChunk;
-    const long long je = min((long long)seg_e, jb + kChunk);
+    const long long jb = (long long)seg_b + (long long)chunk * a.chunk;
+    const long long je = min((long long)seg_e, jb + a.chunk);
     const int np = (int)(je - jb);
     const int nbatch = (np + kPB - 1) / kPB;
 
@@ -411,7 +412,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       for (int r = 0; r < R; ++r) acc[r] += fmaf(beta1, I[1][r], beta0 * I[0][r]);
     }
 
-    const int nch = cnt_s <= kChunk ? 1 : (cnt_s + kChunk - 1) / kChunk;
+    const int nch = cnt_s <= a.chunk ? 1 : (cnt_s + a.chunk - 1) / a.chunk;
     bool have_final = true;
     if (nch > 1) {
       float* part = a.partials + (long long)item * n_t;
@@ -493,7 +494,9 @@ using namespace rubix;
 extern "C" size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
                                             int32_t n_met, int32_t n_age, int32_t n_wave) {
   if (n < 0 || n_segments < 0 || n_wave_t < 0 || n_met < 0 || n_age < 0 || n_wave < 0) return 0;
-  return carve_cube(nullptr, n, n_segments, n_wave_t, n_met, n_age, n_wave).bytes;
+  return carve_cube(nullptr, n, n_segments, n_wave_t, n_met, n_age, n_wave,
+                    cube_tuning_current().chunk)
+      .bytes;
 }
 
 extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,
@@ -542,12 +545,14 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
                 n_wave, SL.total);
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const CubeLayout L = carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave);
+  const CubeTuning tune = cube_tuning_current();
+  const CubeLayout L =
+      carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave, tune.chunk);
   const CubeInputs in{ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met, n_age, n_wave,
                       wave_t, n_wave_t, mass, metallicity, age, velocity, vel_stride,
                       vel_component, perm, seg_offsets, n_segments, n};
   {
-    const int rc = cube_prepare(in, L, /*with_grad=*/false, st);
+    const int rc = cube_prepare(in, L, tune, /*with_grad=*/false, st);
     if (rc != RUBIX_OK) return rc;
   }
   MainArgs args;
@@ -570,6 +575,7 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
   args.ctrl = L.ctrl;
   args.bucket = L.bucket;
   args.row_cap = row_cap;
+  args.chunk = tune.chunk;
   args.lsf_k = n_lsf_taps;
   args.lsf_crop = lsf_crop;
   for (int i = 0; i <= kMaxLsfTaps; ++i) args.lsf[i] = i < n_lsf_taps ? lsf_taps[i] : 0.f;

@@ -51,6 +51,7 @@ struct AdjArgs {
   CubeCtrl* ctrl;
   const int2* bucket;
   int row_cap;
+  int chunk;
 };
 
 struct AdjSmem {
@@ -68,7 +69,7 @@ __host__ __device__ inline AdjSmem adj_smem_layout(int n_wave, int n_grid, int r
   L.row_a = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
   L.row_b = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
   L.red = o;    o = al(o + sizeof(float) * 2 * kAdjWarps * kAdjSums);
-  L.rec = o;    o = al(o + sizeof(ParticleRec) * kChunk);
+  L.rec = o;    o = al(o + sizeof(ParticleRec) * kMaxChunk);
   L.total = o;
   return L;
 }
@@ -277,8 +278,8 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
     const int2 it = a.items[item];
     const int s = it.x, chunk = it.y;
     const int seg_b = a.seg_off[s], seg_e = a.seg_off[s + 1];
-    const long long jb = (long long)seg_b + (long long)chunk * kChunk;
-    const long long je = min((long long)seg_e, jb + kChunk);
+    const long long jb = (long long)seg_b + (long long)chunk * a.chunk;
+    const long long je = min((long long)seg_e, jb + a.chunk);
     const int np = (int)(je - jb);
     const float* adj = a.adj + (long long)s * a.adj_stride;
 #pragma unroll
@@ -384,7 +385,9 @@ using namespace rubix;
 extern "C" size_t rubix_cube_bwd_workspace_size(int64_t n, int32_t n_segments, int32_t n_wave_t,
                                                 int32_t n_met, int32_t n_age, int32_t n_wave) {
   if (n < 0 || n_segments < 0 || n_wave_t < 0 || n_met < 0 || n_age < 0 || n_wave < 0) return 0;
-  return carve_cube(nullptr, n, n_segments, n_wave_t, n_met, n_age, n_wave).bytes;
+  return carve_cube(nullptr, n, n_segments, n_wave_t, n_met, n_age, n_wave,
+                    cube_tuning_current().chunk)
+      .bytes;
 }
 
 extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicity,
@@ -428,12 +431,14 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
                 "(limit 232448)",
                 n_wave, SL.total);
 
-  const CubeLayout L = carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave);
+  const CubeTuning tune = cube_tuning_current();
+  const CubeLayout L =
+      carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave, tune.chunk);
   const CubeInputs in{ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met, n_age, n_wave,
                       wave_t, n_wave_t, mass, metallicity, age, velocity, vel_stride,
                       vel_component, perm, seg_offsets, n_segments, n};
   {
-    const int rc = cube_prepare(in, L, /*with_grad=*/true, st);
+    const int rc = cube_prepare(in, L, tune, /*with_grad=*/true, st);
     if (rc != RUBIX_OK) return rc;
   }
   AdjArgs args;
@@ -460,6 +465,7 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
   args.ctrl = L.ctrl;
   args.bucket = L.bucket;
   args.row_cap = row_cap;
+  args.chunk = tune.chunk;
   const int need_r = (n_wave_t + kAdjThreads - 1) / kAdjThreads;
   const size_t smem = SL.total;
   if (need_r <= 1) return launch_adjoint<1>(args, smem, st);

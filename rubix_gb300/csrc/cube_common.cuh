@@ -9,13 +9,21 @@
 #include "scan.cuh"
 
 namespace rubix {
+
+// Work-item tuning of the cube kernels, per device (tuning.cu; rubix_cube_tuning_set).
+struct CubeTuning {
+  int chunk;     // particles per work item, 32..256, multiple of 32
+  int big_item;  // single-chunk spaxels with at least this many particles go first
+};
+CubeTuning cube_tuning_current();  // of the current device
+
 namespace {
 
 constexpr int kAccThreads = 384;  // forward kernel: 2 blocks of 12 warps per SM
 constexpr int kAccWarps = kAccThreads / 32;
 constexpr int kPB = 2;          // particles per batch (the block reduction packs 2x2 values)
-constexpr int kChunk = 256;     // particles per work item
-constexpr int kBigItem = 64;    // single-chunk spaxels with at least this many go first
+constexpr int kMaxChunk = 256;  // largest work item (particles); records staged per item
+constexpr int kMinChunk = 32;
 constexpr int kBuckets = 1024;  // log-wavelength bucket table entries
 constexpr double kVmaxKms = 10000.0;  // bucket table and one-step-walk check sized for this
 constexpr int kMaxWaveT = 4096;  // telescope wavelengths per spectrum
@@ -245,22 +253,22 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
 
 // Per spaxel: chunk count.  Multi-chunk spaxels get one item (and partial slot) per
 // chunk; single-chunk spaxels are split into a "big" and a "small" class.
-__global__ void cube_count_kernel(const int* __restrict__ seg_off, int n_seg,
-                                  int* __restrict__ slot_cnt, int* __restrict__ big_cnt,
-                                  int* __restrict__ small_cnt) {
+__global__ void cube_count_kernel(const int* __restrict__ seg_off, int n_seg, int chunk,
+                                  int big_item, int* __restrict__ slot_cnt,
+                                  int* __restrict__ big_cnt, int* __restrict__ small_cnt) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_seg; s += gridDim.x * blockDim.x) {
     const int cnt = seg_off[s + 1] - seg_off[s];
-    const int nch = cnt <= kChunk ? 1 : (cnt + kChunk - 1) / kChunk;
+    const int nch = cnt <= chunk ? 1 : (cnt + chunk - 1) / chunk;
     slot_cnt[s] = nch > 1 ? nch : 0;
-    big_cnt[s] = (nch == 1 && cnt >= kBigItem) ? 1 : 0;
-    small_cnt[s] = (nch == 1 && cnt < kBigItem) ? 1 : 0;
+    big_cnt[s] = (nch == 1 && cnt >= big_item) ? 1 : 0;
+    small_cnt[s] = (nch == 1 && cnt < big_item) ? 1 : 0;
   }
 }
 
 // Item order: chunks of multi-chunk spaxels (item index = partial slot), then big
 // single-chunk spaxels, then the rest.
-__global__ void cube_fill_items_kernel(const int* __restrict__ seg_off, int n_seg,
-                                       const int* __restrict__ slot_start,
+__global__ void cube_fill_items_kernel(const int* __restrict__ seg_off, int n_seg, int chunk,
+                                       int big_item, const int* __restrict__ slot_start,
                                        const int* __restrict__ big_start,
                                        const int* __restrict__ small_start,
                                        int2* __restrict__ items, CubeCtrl* __restrict__ ctrl) {
@@ -268,10 +276,10 @@ __global__ void cube_fill_items_kernel(const int* __restrict__ seg_off, int n_se
   const int total_big = big_start[n_seg];
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_seg; s += gridDim.x * blockDim.x) {
     const int cnt = seg_off[s + 1] - seg_off[s];
-    if (cnt > kChunk) {
-      const int nch = (cnt + kChunk - 1) / kChunk;
+    if (cnt > chunk) {
+      const int nch = (cnt + chunk - 1) / chunk;
       for (int c = 0; c < nch; ++c) items[slot_start[s] + c] = make_int2(s, c);
-    } else if (cnt >= kBigItem) {
+    } else if (cnt >= big_item) {
       items[total_slots + big_start[s]] = make_int2(s, 0);
     } else {
       items[total_slots + total_big + small_start[s]] = make_int2(s, 0);
@@ -297,9 +305,10 @@ struct CubeLayout {
   size_t bytes;
 };
 
-long long max_slots(long long n) { return 2 * ((n + kChunk - 1) / kChunk); }
+long long max_slots(long long n, int chunk) { return 2 * ((n + chunk - 1) / chunk); }
 
-CubeLayout carve_cube(void* ws, long long n, int n_seg, int n_t, int nZ, int nA, int nW) {
+CubeLayout carve_cube(void* ws, long long n, int n_seg, int n_t, int nZ, int nA, int nW,
+                      int chunk) {
   Carve c(ws);
   CubeLayout L;
   L.ctrl = c.take<CubeCtrl>(1);
@@ -311,12 +320,15 @@ CubeLayout carve_cube(void* ws, long long n, int n_seg, int n_t, int nZ, int nA,
   L.slot_cnt = c.take<int>((size_t)n_seg + 1);
   L.big_cnt = c.take<int>((size_t)n_seg + 1);
   L.small_cnt = c.take<int>((size_t)n_seg + 1);
-  L.items = c.take<int2>((size_t)(max_slots(n) + n_seg));
+  L.items = c.take<int2>((size_t)(max_slots(n, chunk) + n_seg));
   L.done = c.take<int>((size_t)n_seg);
-  L.partials = c.take<float>((size_t)max_slots(n) * n_t);
+  L.partials = c.take<float>((size_t)max_slots(n, chunk) * n_t);
   L.bytes = c.off;
   return L;
 }
+
+// Work-item tuning of the cube kernels (set per device through rubix_cube_tuning_set;
+// defined in tuning.cu).
 
 // Everything the setup passes read: the SSP grid, the telescope grid and the
 // spaxel-sorted particles.
@@ -343,8 +355,8 @@ struct CubeInputs {
 // Launches the setup passes into the carved workspace: bucket table, corner table,
 // prefix sums, particle records (with dT/dZ, dT/dage when with_grad) and the work-item
 // list.  Six to eight kernels plus three small memsets on stream st.
-inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, bool with_grad,
-                        cudaStream_t st) {
+inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, const CubeTuning& tune,
+                        bool with_grad, cudaStream_t st) {
   RUBIX_CUDA_TRY(cudaMemsetAsync(&L.ctrl->dz_min_bits, 0xff, sizeof(unsigned), st));
   RUBIX_CUDA_TRY(cudaMemsetAsync(&L.ctrl->dt_max_bits, 0, sizeof(unsigned), st));
   {
@@ -375,8 +387,8 @@ inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, bool with_gra
   }
   {
     const int g = (int)std::min<long long>((in.n_seg + 255) / 256, (long long)sm_count() * 8);
-    cube_count_kernel<<<g, 256, 0, st>>>(in.seg_off, in.n_seg, L.slot_cnt, L.big_cnt,
-                                         L.small_cnt);
+    cube_count_kernel<<<g, 256, 0, st>>>(in.seg_off, in.n_seg, tune.chunk, tune.big_item,
+                                         L.slot_cnt, L.big_cnt, L.small_cnt);
     RUBIX_LAUNCH_CHECK("cube_count_kernel");
     scan_exclusive_1block<<<1, 1024, 0, st>>>(L.slot_cnt, in.n_seg, 1);
     RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
@@ -384,7 +396,8 @@ inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, bool with_gra
     RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
     scan_exclusive_1block<<<1, 1024, 0, st>>>(L.small_cnt, in.n_seg, 1);
     RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
-    cube_fill_items_kernel<<<g, 256, 0, st>>>(in.seg_off, in.n_seg, L.slot_cnt, L.big_cnt,
+    cube_fill_items_kernel<<<g, 256, 0, st>>>(in.seg_off, in.n_seg, tune.chunk,
+                                              tune.big_item, L.slot_cnt, L.big_cnt,
                                               L.small_cnt, L.items, L.ctrl);
     RUBIX_LAUNCH_CHECK("cube_fill_items_kernel");
     RUBIX_CUDA_TRY(cudaMemsetAsync(L.done, 0, sizeof(int) * (size_t)in.n_seg, st));

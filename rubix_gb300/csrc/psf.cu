@@ -112,24 +112,30 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// The strip (bx, by) of one cube: ny x nx spaxels (spaxel strides sin/sout), nl
+// wavelengths, taps ty/tx (M each, any address space), 'same' offsets oy/ox.
 template <int M>
-__global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
+__device__ __forceinline__ void psf_reg_body(const float* __restrict__ in, float* __restrict__ out,
+                                             int ny, int nx, int nl, long long sin,
+                                             long long sout, int oy, int ox,
+                                             const float* ty_src, const float* tx_src, int bx,
+                                             int by) {
   constexpr int W = kPsfTileX + M - 1;  // staged row width
   constexpr int PER = (W * kPsfTileL + kPsfThreads - 1) / kPsfThreads;
   __shared__ float s_in[kPsfStages][W * kPsfTileL];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int x0 = blockIdx.x * kPsfTileX;
-  const int l0 = blockIdx.y * kPsfTileL;
+  const int x0 = bx * kPsfTileX;
+  const int l0 = by * kPsfTileL;
   const int l = l0 + lane;
-  const int xsrc0 = x0 - (M - 1) + a.ox;
+  const int xsrc0 = x0 - (M - 1) + ox;
   const int xb = warp * kPsfXB;  // first local x of this thread
   float ty[M], tx[M];
 #pragma unroll
   for (int i = 0; i < M; ++i) {
-    ty[i] = a.ty[i];
-    tx[i] = a.tx[i];
+    ty[i] = ty_src[i];
+    tx[i] = tx_src[i];
   }
-  const int total = a.ny + a.oy;  // input rows 0 .. ny-1+oy
+  const int total = ny + oy;  // input rows 0 .. ny-1+oy
   // This thread's copies of a staged row: element q = tid + k*256 (column jj = q / 32,
   // lane ll = q % 32) comes from row_base + off[k]; the column/wavelength validity is
   // the same for every row.
@@ -140,21 +146,21 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
     const int q = tid + k * kPsfThreads;
     const int jj = q / kPsfTileL, ll = q % kPsfTileL;
     const int xg = xsrc0 + jj, lg = l0 + ll;
-    const bool ok = q < W * kPsfTileL && xg >= 0 && xg < a.nx && lg < a.nl;
-    off[k] = ok ? (int)((long long)xg * a.sin + lg) : 0;
+    const bool ok = q < W * kPsfTileL && xg >= 0 && xg < nx && lg < nl;
+    off[k] = ok ? (int)((long long)xg * sin + lg) : 0;
     valid |= ok ? (1u << k) : 0u;
   }
-  const long long row_stride = (long long)a.nx * a.sin;
+  const long long row_stride = (long long)nx * sin;
   auto issue_row = [&](int r) {
     float* dst = s_in[r % kPsfStages];
-    const float* base = a.in + (long long)r * row_stride;
-    const bool row_ok = r < a.ny;
+    const float* base = in + (long long)r * row_stride;
+    const bool row_ok = r < ny;
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       const int q = tid + k * kPsfThreads;
       if (q < W * kPsfTileL) {
         const bool ok = row_ok && ((valid >> k) & 1u);
-        cp_async4(dst + q, ok ? base + off[k] : a.in, ok);
+        cp_async4(dst + q, ok ? base + off[k] : in, ok);
       }
     }
   };
@@ -194,20 +200,59 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
         win[jj][j] = h;
       }
       // y-pass: output row y = r - oy uses x-convolved rows r - i, i < M
-      const int y = r - a.oy;
-      if (y >= 0 && l < a.nl) {
+      const int y = r - oy;
+      if (y >= 0 && l < nl) {
 #pragma unroll
         for (int j = 0; j < kPsfXB; ++j) {
           float o = 0.f;
 #pragma unroll
           for (int i = 0; i < M; ++i) o = fmaf(ty[i], win[(jj - i + M) % M][j], o);
           const int x = x0 + xb + j;
-          if (x < a.nx) a.out[((long long)y * a.nx + x) * a.sout + l] = o;
+          if (x < nx) out[((long long)y * nx + x) * sout + l] = o;
         }
       }
     }
   }
   cp_async_wait<0>();
+}
+
+template <int M>
+__global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
+  psf_reg_body<M>(a.in, a.out, a.ny, a.nx, a.nl, a.sin, a.sout, a.oy, a.ox, a.ty, a.tx,
+                  blockIdx.x, blockIdx.y);
+}
+
+// Ragged batch: galaxy g owns blocks [block_off[g], block_off[g+1]) (x strips fastest),
+// its square S_g x S_g cube starts at spaxel seg_base[g], and its taps are
+// taps[g][0][:] (y) and taps[g][1][:] (x), zero-padded and centred to M.
+struct RaggedPsfArgs {
+  const float* in;
+  float* out;
+  int nl;
+  long long sin, sout;
+  int n_gal;
+  const int* sbin;
+  const long long* seg_base;
+  const int* block_off;
+  const float* taps;
+};
+
+template <int M>
+__global__ void __launch_bounds__(kPsfThreads) ragged_psf_kernel(RaggedPsfArgs a) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = a.n_gal;  // galaxy: last g with block_off[g] <= b
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (a.block_off[mid] <= b) lo = mid; else hi = mid;
+  }
+  const int g = lo;
+  const int S = a.sbin[g];
+  const int nsx = (S + kPsfTileX - 1) / kPsfTileX;
+  const int local = b - a.block_off[g];
+  const long long base = a.seg_base[g];
+  const float* t = a.taps + (long long)g * 2 * M;
+  psf_reg_body<M>(a.in + base * a.sin, a.out + base * a.sout, S, S, a.nl, a.sin, a.sout,
+                  (M - 1) / 2, (M - 1) / 2, t, t + M, local % nsx, local / nsx);
 }
 
 template <int M>
@@ -280,5 +325,49 @@ extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx
   dim3 grid(div_up(nx, kPsfTileX), div_up(n_wave_t, kPsfTileL));
   psf_strip_kernel<<<grid, kPsfThreads, smem, st>>>(a);
   RUBIX_LAUNCH_CHECK("psf_strip_kernel");
+  return RUBIX_OK;
+}
+
+extern "C" int rubix_ragged_psf_fwd(const float* in, float* out, int32_t n_wave_t,
+                                    int64_t spaxel_stride_in, int64_t spaxel_stride_out,
+                                    int32_t n_gal, const int32_t* sbin, const int64_t* seg_base,
+                                    const int32_t* block_offsets, int32_t n_blocks,
+                                    const float* taps, int32_t m, void* stream) {
+  RUBIX_REQUIRE(n_gal >= 0 && n_wave_t >= 0 && n_blocks >= 0, RUBIX_E_SHAPE,
+                "rubix_ragged_psf_fwd: negative size");
+  RUBIX_REQUIRE(m >= 1 && m <= 21 && (m & 1), RUBIX_E_SHAPE,
+                "rubix_ragged_psf_fwd: padded tap count must be odd and <= 21, got %d", m);
+  RUBIX_REQUIRE(spaxel_stride_in >= n_wave_t && spaxel_stride_out >= n_wave_t, RUBIX_E_SHAPE,
+                "rubix_ragged_psf_fwd: spaxel stride smaller than n_wave_t");
+  if (n_gal == 0 || n_wave_t == 0 || n_blocks == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(in && out && sbin && seg_base && block_offsets && taps, RUBIX_E_INVALID,
+                "rubix_ragged_psf_fwd: null pointer");
+  RUBIX_REQUIRE(in != out, RUBIX_E_INVALID, "rubix_ragged_psf_fwd: in and out must differ");
+  RUBIX_REQUIRE(64LL * spaxel_stride_in < (1LL << 31), RUBIX_E_SHAPE,
+                "rubix_ragged_psf_fwd: spaxel stride too large");
+  RaggedPsfArgs a{in, out, n_wave_t, spaxel_stride_in, spaxel_stride_out, n_gal, sbin,
+                  reinterpret_cast<const long long*>(seg_base), block_offsets, taps};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  switch (m) {
+#define RUBIX_RAGGED_PSF(MM)                                              \
+  case MM:                                                                \
+    ragged_psf_kernel<MM><<<n_blocks, kPsfThreads, 0, st>>>(a);           \
+    break;
+    RUBIX_RAGGED_PSF(1)
+    RUBIX_RAGGED_PSF(3)
+    RUBIX_RAGGED_PSF(5)
+    RUBIX_RAGGED_PSF(7)
+    RUBIX_RAGGED_PSF(9)
+    RUBIX_RAGGED_PSF(11)
+    RUBIX_RAGGED_PSF(13)
+    RUBIX_RAGGED_PSF(15)
+    RUBIX_RAGGED_PSF(17)
+    RUBIX_RAGGED_PSF(19)
+    RUBIX_RAGGED_PSF(21)
+#undef RUBIX_RAGGED_PSF
+    default:
+      break;
+  }
+  RUBIX_LAUNCH_CHECK("ragged_psf_kernel");
   return RUBIX_OK;
 }
