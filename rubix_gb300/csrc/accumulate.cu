@@ -14,16 +14,17 @@
 //     persistent kernel from an atomic counter.  A block of 384 threads owns the
 //     telescope grid of its spaxel: thread i holds R consecutive wavelengths
 //     t = i*R + r in registers (wavelength, bin width, accumulator).
-//   * Per batch of kPB particles the block builds, per particle, the row of entries
-//     (lambda'_k, slope_k, G_k, lambda'_{k+1}) of the mixed template G = sum_c w_c F_c
-//     over the particle's bracket range, reading the corners from the L2-resident corner
-//     table.  Rows are double-buffered: while the block evaluates batch b it builds
-//     batch b+1, so each batch costs one barrier.  The in-range flux sum T
+//   * Per batch of kPB particles one thread issues a 1-D TMA bulk copy of each
+//     particle's corner-table segment (its bracket range only) into shared memory; it
+//     completes on an mbarrier while the block evaluates the previous batch.  The block
+//     then builds per particle the row of entries (lambda'_k, slope_k, G_k,
+//     lambda'_{k+1}) of the mixed template G = sum_c w_c F_c; the in-range flux sum T
 //     (rubix/spectra/ifu.py:241-245) comes from the gather (prefix sums).
 //   * Evaluation: each thread finds the exact bracket of its first wavelength (bucket
 //     table + exact comparisons on lambda') and walks forward over its R wavelengths;
 //     when every SSP interval is wider than every telescope bin the walk advances at
-//     most once per wavelength (one predicated load).  Interpolated values stay in
+//     most once per wavelength (one predicated load); the two particles of a batch are
+//     evaluated interleaved for instruction-level parallelism.  Interpolated values stay in
 //     registers while T' = sum_t I_t dlambda_t is reduced over the block; then
 //     s = nan_to_num(T/T') and the accumulators take mass * s * I.
 //   * Spaxels with more than `chunk` particles are split; each chunk writes a partial
@@ -32,6 +33,7 @@
 //   * Optional epilogue: the LSF convolution along wavelength of the finished spectrum
 //     (rubix/telescope/lsf/lsf.py:29-105), which commutes with the PSF.
 #include "cube_common.cuh"
+#include "tma.cuh"
 
 namespace rubix {
 namespace {
@@ -59,10 +61,10 @@ struct MainArgs {
   float lsf[kMaxLsfTaps + 1];
 };
 
-// Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned).  The rows
-// are double-buffered: [2][kPB][row_cap] entries.
+// Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned): the TMA
+// staging of a batch's corner segments [kPB][row_cap] and its rows [kPB][row_cap].
 struct SmemLayout {
-  size_t wz, bucket, rows, red, rec, total;
+  size_t wz, bucket, stage, rows, red, rec, total;
 };
 
 __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
@@ -71,8 +73,9 @@ __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
   auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
   L.wz = o;     o = al(o + sizeof(float) * n_wave);
   L.bucket = o; o = al(o + sizeof(int2) * kBuckets);
+  L.stage = o;  o = al(o + sizeof(float4) * kPB * (size_t)row_cap);
   L.rows = o;   // also holds the zero-padded spectrum of the LSF epilogue
-  o = al(o + std::max(sizeof(float4) * 2 * kPB * (size_t)row_cap,
+  o = al(o + std::max(sizeof(float4) * kPB * (size_t)row_cap,
                       sizeof(float) * (size_t)(kMaxWaveT + 2 * kMaxLsfTaps + 8)));
   L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 2);
   L.rec = o;    o = al(o + sizeof(ParticleRec) * kMaxChunk);
@@ -80,16 +83,45 @@ __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
   return L;
 }
 
+// Thread 0: arm the barrier and issue one bulk copy per particle of the batch: the
+// corner-table entries k in [max(kstart,0), min(kend+1, nW-1)] of its cell.
+__device__ __forceinline__ void issue_stage(const MainArgs& a, const ParticleRec* recs, int cnt,
+                                            float4* stage, uint64_t* bar) {
+  fence_proxy_async_smem();  // earlier generic reads of the staging buffer come first
+  uint32_t bytes = 0;
+  int klo[kPB], nk[kPB], cells[kPB];
+#pragma unroll
+  for (int p = 0; p < kPB; ++p) {
+    cells[p] = -1;
+    klo[p] = 0;
+    nk[p] = 0;
+    if (p < cnt) {
+      const int4 b = recs[p].b;
+      const int ks = b.y, ke = b.z & ~kGenericFlag;
+      klo[p] = max(ks, 0);
+      nk[p] = min(ke + 1, a.n_wave - 1) - klo[p] + 1;
+      cells[p] = b.x;
+      if (b.x >= 0) bytes += 16u * (uint32_t)nk[p];
+    }
+  }
+  mbar_arrive_expect_tx(bar, bytes);
+#pragma unroll
+  for (int p = 0; p < kPB; ++p)
+    if (cells[p] >= 0)
+      bulk_copy_g2s(stage + (size_t)p * a.row_cap, a.ct + (long long)cells[p] * a.n_wave + klo[p],
+                    16u * nk[p], bar);
+}
+
 struct RowParams {
   float alpha, w00, w10, w01, w11;
   int ks, klo, khi, n_e;
   bool has_cell;
-  const float4* ct;  // ct[k] = corners of SSP wavelength k of the particle's cell (global)
+  const float4* st;  // st[k] = staged corners of SSP wavelength k
   float4* row;
 };
 
 __device__ __forceinline__ RowParams row_params(const ParticleRec& r, const MainArgs& a,
-                                                float4* row) {
+                                                const float4* stage, float4* row) {
   RowParams q;
   const float tz = r.a.w, ta = __int_as_float(r.b.w);
   const int ke = r.b.z & ~kGenericFlag;
@@ -103,7 +135,7 @@ __device__ __forceinline__ RowParams row_params(const ParticleRec& r, const Main
   q.khi = min(ke + 1, a.n_wave - 1);
   q.n_e = ke - q.ks + 1;
   q.has_cell = r.b.x >= 0;
-  q.ct = a.ct + (long long)(q.has_cell ? r.b.x : 0) * a.n_wave;
+  q.st = stage - q.klo;
   q.row = row;
   return q;
 }
@@ -111,7 +143,7 @@ __device__ __forceinline__ RowParams row_params(const ParticleRec& r, const Main
 // One warp step of a row build: entries base .. base+30 (lane 31 supplies the right
 // neighbour).  Entry e (SSP index k = kstart + e) = (lambda'_k, slope_k, G_k,
 // lambda'_{k+1}), with sentinels (-FLT_MAX, 0, G_0, lambda'_0) for k = -1 and
-// slope 0 / FLT_MAX beyond the grid.  The corners come from the L2-resident table.
+// slope 0 / FLT_MAX beyond the grid.  The corners come from the staged segment.
 __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
                                            const float* __restrict__ s_wz, int lane) {
   const int e = base + lane;
@@ -120,7 +152,7 @@ __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
     // interior step: every lane, neighbour included, is an SSP wavelength of the range
     float G = 0.f;
     if (q.has_cell) {
-      const float4 c = __ldg(q.ct + k);
+      const float4 c = q.st[k];
       G = q.w00 * c.x;
       G = fmaf(q.w10, c.y, G);
       G = fmaf(q.w01, c.z, G);
@@ -138,7 +170,7 @@ __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
     const int kk = min(max(k, q.klo), q.khi);
     float G = 0.f;
     if (q.has_cell) {
-      const float4 c = __ldg(q.ct + kk);
+      const float4 c = q.st[kk];
       G = q.w00 * c.x;
       G = fmaf(q.w10, c.y, G);
       G = fmaf(q.w01, c.z, G);
@@ -159,18 +191,60 @@ __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
   }
 }
 
+// Interior build steps of two particles at the same base, interleaved: both particles'
+// corner loads, mixes, shuffles and slopes are independent, so their latencies overlap.
+__device__ __forceinline__ bool interior(const RowParams& q, int base) {
+  return q.ks + base >= 0 && q.ks + base + 31 <= q.khi;
+}
+
+__device__ __forceinline__ void build_step_pair(const RowParams& q0, const RowParams& q1,
+                                                int base, const float* __restrict__ s_wz,
+                                                int lane) {
+  const int e = base + lane;
+  const int k0 = q0.ks + e, k1 = q1.ks + e;
+  const float4 c0 = q0.st[k0];
+  const float4 c1 = q1.st[k1];
+  const float z0 = s_wz[k0], z1 = s_wz[k1];
+  float G0 = q0.w00 * c0.x, G1 = q1.w00 * c1.x;
+  G0 = fmaf(q0.w10, c0.y, G0);
+  G1 = fmaf(q1.w10, c1.y, G1);
+  G0 = fmaf(q0.w01, c0.z, G0);
+  G1 = fmaf(q1.w01, c1.z, G1);
+  G0 = fmaf(q0.w11, c0.w, G0);
+  G1 = fmaf(q1.w11, c1.w, G1);
+  if (!q0.has_cell) G0 = 0.f;
+  if (!q1.has_cell) G1 = 0.f;
+  const float lp0 = __fmul_rn(z0, q0.alpha), lp1 = __fmul_rn(z1, q1.alpha);
+  const float lpn0 = __shfl_down_sync(0xffffffffu, lp0, 1);
+  const float lpn1 = __shfl_down_sync(0xffffffffu, lp1, 1);
+  const float Gn0 = __shfl_down_sync(0xffffffffu, G0, 1);
+  const float Gn1 = __shfl_down_sync(0xffffffffu, G1, 1);
+  if (lane < 31) {
+    const float dl0 = lpn0 - lp0, dl1 = lpn1 - lp1;
+    const float sl0 = dl0 > 0.f ? __fdividef(Gn0 - G0, dl0) : 0.f;
+    const float sl1 = dl1 > 0.f ? __fdividef(Gn1 - G1, dl1) : 0.f;
+    q0.row[e] = make_float4(lp0, sl0, G0, lpn0);
+    q1.row[e] = make_float4(lp1, sl1, G1, lpn1);
+  }
+}
+
 // Builds the rows of the (one or two) particles of a batch into `rows`
-// ([kPB][row_cap]), interleaving their steps.
+// ([kPB][row_cap]) from the staged corners, interleaving their steps.
 __device__ __forceinline__ void build_rows(const MainArgs& a, const ParticleRec* recs, int cnt,
                                            const float* __restrict__ s_wz,
+                                           const float4* __restrict__ stage,
                                            float4* __restrict__ rows, int lane, int warp) {
-  const RowParams q0 = row_params(recs[0], a, rows);
+  const RowParams q0 = row_params(recs[0], a, stage, rows);
   if (cnt > 1) {
-    const RowParams q1 = row_params(recs[1], a, rows + a.row_cap);
+    const RowParams q1 = row_params(recs[1], a, stage + a.row_cap, rows + a.row_cap);
     const int n_max = max(q0.n_e, q1.n_e);
     for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
-      if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
-      if (base < q1.n_e) build_step(q1, base, a.n_wave, s_wz, lane);
+      if (base < q0.n_e && base < q1.n_e && interior(q0, base) && interior(q1, base)) {
+        build_step_pair(q0, q1, base, s_wz, lane);
+      } else {
+        if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
+        if (base < q1.n_e) build_step(q1, base, a.n_wave, s_wz, lane);
+      }
     }
   } else {
     for (int base = warp * 31; base < q0.n_e; base += kAccWarps * 31)
@@ -288,25 +362,48 @@ __device__ __forceinline__ void lsf_epilogue(const MainArgs& a, const float* __r
   }
 }
 
+// The same with K taps known at compile time: the R + K - 1 window in registers.
+template <int R, int K>
+__device__ __forceinline__ void lsf_epilogue_k(const MainArgs& a,
+                                               const float* __restrict__ s_pad, int t0,
+                                               float (&out)[R]) {
+  float win[R + K - 1];
+#pragma unroll
+  for (int i = 0; i < R + K - 1; ++i) win[i] = s_pad[t0 + i];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    float o = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) o = fmaf(a.lsf[j], win[r + K - 1 - j], o);
+    out[r] = o;
+  }
+}
+
 template <int R>
 __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout SL = smem_layout(a.n_wave, a.row_cap);
   float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
   int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
-  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);        // [2][kPB][row_cap]
+  float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);      // [kPB][row_cap]
+  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);        // [kPB][row_cap]
   float* s_red = reinterpret_cast<float*>(smem + SL.red);            // [2][warps][2]
   ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);  // records of the item
   float* s_spec = reinterpret_cast<float*>(s_rows);  // LSF epilogue reuses the rows
-  __shared__ int s_item, s_last;
+  __shared__ uint64_t s_bar;
+  __shared__ int s_item, s_last, s_fail;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int i = tid; i < a.n_wave; i += kAccThreads) s_wz[i] = a.wave_z[i];
   for (int b = tid; b < kBuckets; b += kAccThreads) s_bucket[b] = a.bucket[b];
+  if (tid == 0) {
+    mbar_init(&s_bar, 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
 
   const int n_t = a.n_t;
   const int t0 = tid * R;
-  const size_t buf_stride = (size_t)kPB * a.row_cap;
   float lam[R], dlam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -317,6 +414,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   }
   const float A0 = a.At[t0 < n_t ? t0 : n_t - 1];
   const int n_items = a.ctrl->n_items;
+  uint32_t phase = 0;
   __syncthreads();
 
   for (;;) {
@@ -338,18 +436,28 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
     // records of this item into shared memory (one 48-byte record per thread)
     for (int i = tid; i < np; i += kAccThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
-    if (nbatch > 0) build_rows(a, s_rec, min(kPB, np), s_wz, s_rows, lane, warp);
-    __syncthreads();  // rows of batch 0 ready
+    if (nbatch > 0 && tid == 0) issue_stage(a, s_rec, min(kPB, np), s_stage, &s_bar);
 
-    // Batch bt: build batch bt+1 into the other buffer, evaluate batch bt, one barrier.
+    // Batch bt: wait for its staged corners, build its rows, issue the next batch's
+    // copies, evaluate, reduce T'.
     for (int bt = 0; bt < nbatch; ++bt) {
       const int buf = bt & 1;
       const int cnt = min(kPB, np - bt * kPB);
       const ParticleRec* recs = s_rec + bt * kPB;
-      if (bt + 1 < nbatch)
-        build_rows(a, recs + kPB, min(kPB, np - (bt + 1) * kPB), s_wz,
-                   s_rows + (buf ^ 1) * buf_stride, lane, warp);
-      const float4* rows = s_rows + buf * buf_stride;
+      if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
+      phase ^= 1u;
+      build_rows(a, recs, cnt, s_wz, s_stage, s_rows, lane, warp);
+      __syncthreads();  // rows ready; staging consumed
+      if (s_fail) {
+        if (tid == 0) {
+          atomicExch(&a.ctrl->error, 1);
+          mbar_wait_bounded(&s_bar, phase ^ 1u);  // give copies in flight a last chance
+        }
+        return;
+      }
+      if (bt + 1 < nbatch && tid == 0)
+        issue_stage(a, recs + kPB, min(kPB, np - (bt + 1) * kPB), s_stage, &s_bar);
+      const float4* rows = s_rows;
       float I[kPB][R];
       float tp[kPB];
       const float B0 = recs[0].a.z;
@@ -387,7 +495,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       // T'0, T'1 over the warp, then over the block (fixed order: deterministic).
       const float wsum = warp_reduce2(tp[0], tp[1], lane);
       if ((lane & 15) == 0) s_red[(buf * kAccWarps + warp) * 2 + (lane >> 4)] = wsum;
-      __syncthreads();  // partial sums of batch bt and rows of batch bt+1 ready
+      __syncthreads();  // partial sums of batch bt ready; rows free for the next build
       // lanes 0..15 take warp (lane & 15)'s partial of T'0, lanes 16..31 of T'1
       const int wl = lane & 15;
       float v = (wl < kAccWarps) ? s_red[(buf * kAccWarps + wl) * 2 + (lane >> 4)] : 0.f;
@@ -409,7 +517,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       const float beta0 = __shfl_sync(0xffffffffu, beta_l, 0);
       const float beta1 = __shfl_sync(0xffffffffu, beta_l, 16);
 #pragma unroll
-      for (int r = 0; r < R; ++r) acc[r] += fmaf(beta1, I[1][r], beta0 * I[0][r]);
+      for (int r = 0; r < R; ++r) acc[r] = fmaf(beta1, I[1][r], fmaf(beta0, I[0][r], acc[r]));
     }
 
     const int nch = cnt_s <= a.chunk ? 1 : (cnt_s + a.chunk - 1) / a.chunk;
@@ -456,7 +564,10 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
         for (int r = 0; r < R; ++r)
           if (t0 + r < n_t) s_spec[lead + t0 + r] = acc[r];
         __syncthreads();
-        lsf_epilogue<R>(a, s_spec, t0, acc);
+        if (a.lsf_k == 25)  // rubix's LSF: 2 * 12 + 1 taps (telescope/lsf/lsf.py:12-26)
+          lsf_epilogue_k<R, 25>(a, s_spec, t0, acc);
+        else
+          lsf_epilogue<R>(a, s_spec, t0, acc);
       }
 #pragma unroll
       for (int r = 0; r < R; ++r)
