@@ -344,6 +344,35 @@ RUBIX_API int rubix_segmented_dot(const float* a, const float* b, const int64_t*
                                   size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------- */
+/* Observation noise                                                         */
+/* ------------------------------------------------------------------------- */
+/*
+ * apply_noise (rubix/core/noise.py:17-80; calculate_S2N / calculate_noise_cube,
+ * rubix/telescope/noise/noise.py:35-115) in three calls:
+ *   rubix_flux_image:   flux[s] = sum_t cube[s][t]
+ *   rubix_noise_median: *median (device) = median of flux, or 0 when any flux <= 0
+ *                       (rubix's jnp.median over where(flux > 0, flux, nan) is NaN then,
+ *                       and nan_to_num makes it 0)
+ *   rubix_apply_noise:  cube[s][t] += cube[s][t] * z * sqrt(median) / s2n / sqrt(flux[s])
+ *                       (0 where flux <= 0), z ~ N(0,1) (distribution 0) or U[0,1) (1).
+ * rubix draws z from jax.random with a fixed key; here z comes from Philox4x32-10 keyed
+ * by `seed` with the element index as counter: reproducible per seed, equal to rubix's
+ * noise in distribution only.
+ */
+RUBIX_API int rubix_flux_image(const float* cube, int64_t n_spaxels, int32_t n_wave_t,
+                               int64_t spaxel_stride, float* flux, void* stream);
+RUBIX_API size_t rubix_noise_median_workspace_size(void);
+RUBIX_API int rubix_noise_median(const float* flux, int64_t n, float* median, void* workspace,
+                                 size_t workspace_bytes, void* stream);
+RUBIX_API int rubix_apply_noise(float* cube, int64_t n_spaxels, int32_t n_wave_t,
+                                int64_t spaxel_stride, const float* flux, const float* median,
+                                float signal_to_noise, int32_t distribution, uint64_t seed,
+                                void* stream);
+/* No counterpart in rubix: the generator of rubix_apply_noise on the host (one block of
+ * Philox4x32-10: counter[4], key[2] -> out[4]), for checking its output. */
+RUBIX_API int rubix_philox4x32_10(const uint32_t* counter4, const uint32_t* key2, uint32_t* out4);
+
+/* ------------------------------------------------------------------------- */
 /* Tuning                                                                    */
 /* ------------------------------------------------------------------------- */
 /*

@@ -598,6 +598,42 @@ def lsf_taps_derivative(sigma, wave_res, factor=12):
     return t, (de - t * de.sum()) / S
 
 
+# ----------------------------------------------------------------------------------
+# Observation noise (core/noise.py:17-80, telescope/noise/noise.py:35-115)
+# ----------------------------------------------------------------------------------
+def noise_sigma(datacube, signal_to_noise):
+    """calculate_S2N (noise.py:35-76): per-spaxel relative noise
+    sqrt(median flux) / s2n / sqrt(flux), 0 where flux <= 0; the median is over
+    where(flux > 0, flux, nan), so any flux <= 0 makes it NaN -> 0."""
+    cube = np.asarray(datacube, dtype=np.float64)
+    flux = cube.sum(axis=-1)
+    nonzero = flux > 0
+    with np.errstate(invalid="ignore"):
+        med = np.median(np.where(nonzero, flux, np.nan))
+    med = 0.0 if np.isnan(med) else med
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = np.sqrt(med) / signal_to_noise / np.sqrt(flux)
+    return np.where(nonzero, s, 0.0), med
+
+
+def philox4x32_10(counter, key):
+    """Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), pure Python: 10 rounds of
+    two 32x32->64 multiplies with M0 = 0xD2511F53, M1 = 0xCD9E8D57 and a Weyl key
+    schedule W0 = 0x9E3779B9, W1 = 0xBB67AE85."""
+    m = 0xFFFFFFFF
+    c = [int(x) & m for x in counter]
+    k0, k1 = int(key[0]) & m, int(key[1]) & m
+    for _ in range(10):
+        p0 = 0xD2511F53 * c[0]
+        p1 = 0xCD9E8D57 * c[2]
+        c = [((p1 >> 32) ^ c[1] ^ k0) & m, p1 & m, ((p0 >> 32) ^ c[3] ^ k1) & m, p0 & m]
+        k0 = (k0 + 0x9E3779B9) & m
+        k1 = (k1 + 0xBB67AE85) & m
+    return c
+
+
+__all__ += ["noise_sigma", "philox4x32_10"]
+
 __all__ += ["interp2d_linear_grad", "doppler_grid", "particle_objective", "particle_grads",
             "psf_taps_derivative", "lsf_taps_derivative"]
 

@@ -11,6 +11,7 @@ from .data import (Galaxy, GasData, RubixData, StarsData, get_reshape_data,  # n
 from .ifu import (get_calculate_datacube, get_calculate_spectra,  # noqa: F401
                   get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
 from .lsf import get_convolve_lsf  # noqa: F401
+from .noise import get_apply_noise  # noqa: F401
 from .pipeline import RubixPipeline  # noqa: F401
 from .psf import get_convolve_psf  # noqa: F401
 from .ssp import get_lookup_interpolation, get_ssp, register_ssp_template  # noqa: F401

@@ -2,9 +2,9 @@
 
 Differences from rubix, all outside the particle -> cube path: the particle data is
 passed in (``data=``) instead of being read from simulation files; ``rotate_galaxy``
-expects particles already in the observer frame and ``apply_noise`` is not part of
-this package (both raise if their configuration asks for work); the SSP lookup is
-bilinear (``ssp.method = "linear"``).
+expects particles already in the observer frame (it raises if its configuration asks
+for a rotation); the SSP lookup is bilinear (``ssp.method = "linear"``); the noise of
+``apply_noise`` comes from a seeded Philox generator instead of jax.random.
 """
 
 from __future__ import annotations
@@ -19,6 +19,7 @@ from .data import RubixData, get_reshape_data
 from .ifu import (get_calculate_datacube, get_calculate_spectra,
                   get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
 from .lsf import get_convolve_lsf
+from .noise import get_apply_noise
 from .psf import get_convolve_psf
 from .ssp import get_ssp
 from .telescope import get_filter_particles, get_spaxel_assignment, get_telescope
@@ -36,18 +37,6 @@ def get_galaxy_rotation(config: dict):
         return rubixdata
 
     return rotate_galaxy
-
-
-def get_apply_noise(config: dict):
-    """Noise is not part of rubix_gb300; a configured signal-to-noise is refused."""
-    noise = config.get("telescope", {}).get("noise")
-    if noise and noise.get("signal_to_noise") not in (None, 0):
-        raise NotImplementedError("apply_noise is not part of rubix_gb300")
-
-    def apply_noise(rubixdata: RubixData) -> RubixData:
-        return rubixdata
-
-    return apply_noise
 
 
 class RubixPipeline:

@@ -282,6 +282,21 @@ __device__ __forceinline__ int first_bracket(const float4* __restrict__ rowp, in
   return k;
 }
 
+// One-step walk on a row in shared memory, branch-free: if x >= e.w (the right end of
+// the current interval) advance the entry address by one and load the next entry.  The
+// predicate covers the add and the load, so lanes that stay issue no divergent branch.
+__device__ __forceinline__ void walk_step(float x, unsigned& addr, float4& e) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ge.f32 p, %5, %4;\n\t"
+      "@p add.u32 %0, %0, 16;\n\t"
+      "@p ld.shared.v4.f32 {%1, %2, %3, %4}, [%0];\n\t"
+      "}"
+      : "+r"(addr), "+f"(e.x), "+f"(e.y), "+f"(e.z), "+f"(e.w)
+      : "f"(x)
+      : "memory");
+}
+
 // Interpolated values of one particle at this thread's R wavelengths; returns the
 // partial sum of I_t * dlambda_t.
 template <int R, bool kGeneric>
@@ -292,15 +307,15 @@ __device__ __forceinline__ float eval_particle(const float4* __restrict__ rowp, 
                                                float (&I)[R]) {
   float4 e;
   int k = first_bracket(rowp, ks, ke, B, A0, s_bucket, lam[0], e);
+  unsigned addr = static_cast<unsigned>(__cvta_generic_to_shared(rowp + k));
   float tp = 0.f;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const float x = lam[r];
     if (kGeneric) {
       while (k < ke && x >= e.w) { ++k; e = rowp[k]; }
-    } else if (r > 0 && x >= e.w) {
-      ++k;
-      e = rowp[k];
+    } else if (r > 0) {
+      walk_step(x, addr, e);
     }
     const float v = fmaf(x - e.x, e.y, e.z);
     I[r] = v;
@@ -320,22 +335,18 @@ __device__ __forceinline__ void eval_pair(const float4* __restrict__ row0, int k
                                           float (&I0)[R], float (&I1)[R], float& tp0,
                                           float& tp1) {
   float4 e0, e1;
-  int k0 = first_bracket(row0, ks0, ke0, B0, A0, s_bucket, lam[0], e0);
-  int k1 = first_bracket(row1, ks1, ke1, B1, A0, s_bucket, lam[0], e1);
+  const int k0 = first_bracket(row0, ks0, ke0, B0, A0, s_bucket, lam[0], e0);
+  const int k1 = first_bracket(row1, ks1, ke1, B1, A0, s_bucket, lam[0], e1);
+  unsigned a0 = static_cast<unsigned>(__cvta_generic_to_shared(row0 + k0));
+  unsigned a1 = static_cast<unsigned>(__cvta_generic_to_shared(row1 + k1));
   tp0 = 0.f;
   tp1 = 0.f;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const float x = lam[r];
     if (r > 0) {
-      if (x >= e0.w) {
-        ++k0;
-        e0 = row0[k0];
-      }
-      if (x >= e1.w) {
-        ++k1;
-        e1 = row1[k1];
-      }
+      walk_step(x, a0, e0);
+      walk_step(x, a1, e1);
     }
     const float v0 = fmaf(x - e0.x, e0.y, e0.z);
     const float v1 = fmaf(x - e1.x, e1.y, e1.z);

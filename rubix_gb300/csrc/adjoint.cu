@@ -25,7 +25,7 @@
 namespace rubix {
 namespace {
 
-constexpr int kAdjThreads = 256;
+constexpr int kAdjThreads = 384;  // 2 blocks of 12 warps per SM
 constexpr int kAdjWarps = kAdjThreads / 32;
 constexpr int kAdjSums = 8;
 
@@ -157,8 +157,7 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
                                          const float4* __restrict__ rb, int ks, int ke, float B,
                                          float A0, const int2* __restrict__ s_bucket,
                                          const float (&lam)[R], const float (&dlam)[R],
-                                         const float (&h)[R], const float (&hx)[R],
-                                         const float (&dx)[R], float (&s)[kAdjSums]) {
+                                         const float (&h)[R], float (&s)[kAdjSums]) {
   const float u = A0 - B;
   int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
   b = min(max(b, 0), kBuckets - 1);
@@ -196,8 +195,9 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
     s[3] = fmaf(dlam[r], IZ, s[3]);
     s[4] = fmaf(h[r], IA, s[4]);
     s[5] = fmaf(dlam[r], IA, s[5]);
-    s[6] = fmaf(hx[r], e.y, s[6]);
-    s[7] = fmaf(dx[r], e.y, s[7]);
+    const float xs = x * e.y;  // lambda_t * slope
+    s[6] = fmaf(h[r], xs, s[6]);
+    s[7] = fmaf(dlam[r], xs, s[7]);
   }
 }
 
@@ -255,14 +255,13 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
   }
   const int n_t = a.n_t;
   const int t0 = tid * R;
-  float lam[R], dlam[R], dx[R], h[R], hx[R];
+  float lam[R], dlam[R], h[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int t = t0 + r;
     const int tc = t < n_t ? t : n_t - 1;
     lam[r] = a.wave_t[tc];
     dlam[r] = (t < n_t && t > 0) ? (a.wave_t[t] - a.wave_t[t - 1]) : 0.f;
-    dx[r] = dlam[r] * lam[r];
   }
   const float A0 = a.At[t0 < n_t ? t0 : n_t - 1];
   const int n_items = a.ctrl->n_items;
@@ -283,10 +282,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
     const int np = (int)(je - jb);
     const float* adj = a.adj + (long long)s * a.adj_stride;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      h[r] = (t0 + r < n_t) ? adj[t0 + r] : 0.f;
-      hx[r] = h[r] * lam[r];
-    }
+    for (int r = 0; r < R; ++r) h[r] = (t0 + r < n_t) ? adj[t0 + r] : 0.f;
     for (int i = tid; i < np; i += kAdjThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
     if (np > 0 && tid == 0) adj_issue(a, s_rec[0], s_stage, &s_bar);
@@ -310,11 +306,11 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
       const int ks = rb.y, ke = rb.z & ~kGenericFlag;
       float sums[kAdjSums];
       if (rb.z & kGenericFlag)
-        adj_eval<R, true>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h, hx,
-                          dx, sums);
+        adj_eval<R, true>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h,
+                          sums);
       else
-        adj_eval<R, false>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h, hx,
-                           dx, sums);
+        adj_eval<R, false>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h,
+                           sums);
       const float wv = warp_reduce8(sums, lane);
       if ((lane & 3) == 0) {
         const int v = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
@@ -471,8 +467,8 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
   if (need_r <= 1) return launch_adjoint<1>(args, smem, st);
   if (need_r <= 2) return launch_adjoint<2>(args, smem, st);
   if (need_r <= 4) return launch_adjoint<4>(args, smem, st);
+  if (need_r <= 6) return launch_adjoint<6>(args, smem, st);
   if (need_r <= 8) return launch_adjoint<8>(args, smem, st);
-  if (need_r <= 12) return launch_adjoint<12>(args, smem, st);
-  if (need_r <= 15) return launch_adjoint<15>(args, smem, st);
-  return launch_adjoint<16>(args, smem, st);
+  if (need_r <= 10) return launch_adjoint<10>(args, smem, st);
+  return launch_adjoint<11>(args, smem, st);  // kAdjThreads * 11 >= kMaxWaveT
 }

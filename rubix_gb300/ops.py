@@ -23,6 +23,9 @@ __all__ = [
     "lsf_forward",
     "cube_backward",
     "dot",
+    "flux_image",
+    "noise_median",
+    "apply_noise_",
     "workspace",
 ]
 
@@ -224,6 +227,67 @@ def dot(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
               _stream(a.device))
     _count(1)
     return out
+
+
+def flux_image(cube: torch.Tensor) -> torch.Tensor:
+    """[..., L] -> [...] float32: sum over the last axis (the flux image of a cube)."""
+    _check_cuda("cube", cube, torch.float32)
+    L = cube.shape[-1]
+    rows = cube.reshape(-1, L)
+    if rows.stride(-1) != 1:
+        rows = rows.contiguous()
+    out = torch.empty(rows.shape[0], dtype=torch.float32, device=cube.device)
+    _lib.call("rubix_flux_image", _ptr(rows), rows.shape[0], L, rows.stride(0), _ptr(out),
+              _stream(cube.device))
+    _count(1 if rows.shape[0] > 0 else 0)
+    return out.view(cube.shape[:-1])
+
+
+def noise_median(flux: torch.Tensor) -> torch.Tensor:
+    """0-d float32: median of `flux`, or 0 when any value is <= 0 (rubix's
+    nan_to_num(jnp.median(where(flux > 0, flux, nan))))."""
+    _check_cuda("flux", flux, torch.float32)
+    f = flux.contiguous().reshape(-1)
+    out = torch.empty((), dtype=torch.float32, device=f.device)
+    ws = workspace(_lib.query("rubix_noise_median_workspace_size"), f.device)
+    _lib.call("rubix_noise_median", _ptr(f), f.numel(), _ptr(out), _ptr(ws), ws.numel(),
+              _stream(f.device))
+    _count(2 + 8 * (f.numel() > 0))
+    return out
+
+
+def apply_noise_(cube: torch.Tensor, signal_to_noise: float, distribution: str = "normal",
+                 seed: int = 0, flux=None, median=None) -> torch.Tensor:
+    """In place: cube += cube * z * sqrt(median) / s2n / sqrt(flux) per spaxel (rubix's
+    calculate_noise_cube), z from Philox4x32-10 keyed by `seed`."""
+    _check_cuda("cube", cube, torch.float32)
+    if not cube.is_contiguous():
+        raise ValueError("cube must be contiguous")
+    dist = {"normal": 0, "uniform": 1}.get(distribution)
+    if dist is None:
+        raise ValueError(f"Invalid noise type: {distribution}. Supported types: "
+                         "['normal', 'uniform']")
+    L = cube.shape[-1]
+    rows = cube.view(-1, L)
+    flux = flux_image(cube).reshape(-1) if flux is None else flux.reshape(-1)
+    median = noise_median(flux) if median is None else median
+    _lib.call("rubix_apply_noise", _ptr(rows), rows.shape[0], L, rows.stride(0), _ptr(flux),
+              _ptr(median), float(signal_to_noise), dist, int(seed) & (2**64 - 1),
+              _stream(cube.device))
+    _count(1 if rows.numel() > 0 else 0)
+    return cube
+
+
+def philox4x32_10(counter, key) -> list:
+    """One Philox4x32-10 block computed by the library on the host (no GPU needed)."""
+    import ctypes
+
+    c = (ctypes.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in counter])
+    k = (ctypes.c_uint32 * 2)(*[int(x) & 0xFFFFFFFF for x in key])
+    o = (ctypes.c_uint32 * 4)()
+    _lib.call("rubix_philox4x32_10", ctypes.addressof(c), ctypes.addressof(k),
+              ctypes.addressof(o))
+    return [int(x) for x in o]
 
 
 def _host_taps(t) -> np.ndarray:

@@ -22,7 +22,10 @@ def _config(w, name="small_test_ssp"):
         "data": {"args": {"particle_type": ["stars"]}},
         "telescope": {"name": "MUSE", "psf": {"name": "gaussian", "size": w.psf_size,
                                               "sigma": w.psf_sigma},
-                      "lsf": {"sigma": w.lsf_sigma}},
+                      "lsf": {"sigma": w.lsf_sigma},
+                      # S/N so large that the noise cannot change a float32 value: the
+                      # parity comparison is pre-noise
+                      "noise": {"signal_to_noise": 1e30, "noise_distribution": "normal"}},
         "cosmology": {"name": "PLANCK15"},
         "galaxy": {"dist_z": w.dist_z},
         "ssp": {"template": {"name": name}, "method": "linear"},
@@ -50,6 +53,24 @@ def test_rubix_pipeline_matches_oracle():
     assert np.array_equal(out.stars.pixel_assignment.cpu().numpy().reshape(-1),
                           ref["pixel_assignment"])
     assert np.array_equal(out.stars.mask.cpu().numpy().reshape(-1), ref["mask"])
+
+
+def test_rubix_pipeline_noise():
+    """calc_ifu with S/N = 20: the noise step changes the cube by cube * sigma * z."""
+    from rubix_gb300.core import RubixPipeline
+
+    w = workload("small")
+    cfg = _config(w)
+    ref = oracle_stages("small")["final"]
+    cfg["telescope"]["noise"] = {"signal_to_noise": 20, "noise_distribution": "normal"}
+    out = RubixPipeline(cfg, _data(w)).run().stars.datacube.cpu().numpy().astype(np.float64)
+    sig, med = oracle.noise_sigma(ref, 20.0)
+    if med == 0.0:  # an empty spaxel disables rubix's noise (NaN median)
+        assert_cube_close(out, ref, what="noise-free cube")
+        return
+    ok = ref > 1e-3 * np.abs(ref).max()
+    z = ((out - ref) / (ref * sig[:, :, None]))[ok]
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1.0) < 0.01
 
 
 def test_steps_one_by_one_materialised():
