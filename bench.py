@@ -222,7 +222,8 @@ def workload_config(w):
         "n_particles": p.n, "n_spaxels": w.sbin * w.sbin, "n_wave": int(w.wave_t.size),
         "ssp": [int(w.ssp.metallicity.size), int(w.ssp.age.size), int(w.ssp.wavelength.size)],
         "l2": "flushed before every timed step (512 MiB device write)",
-        "path": "mask+assign+sort -> fused accumulate with LSF epilogue -> PSF (LSF and PSF commute)",
+        "path": "mask+assign+sort -> fused accumulate with LSF epilogue -> PSF (LSF and PSF commute)"
+                + (f" -> noise at S/N {w.noise_s2n}" if w.noise_s2n else ""),
     }
 
 
@@ -536,7 +537,7 @@ def main():
         cube = rnd.accumulate(d_in[2], d_in[3], d_in[4], d_in[1], perm, offs, with_lsf=True)
         if ev is not None:
             ev[1].record()
-        return rnd.psf(cube)
+        return rnd.noise_(rnd.psf(cube))
 
     for _ in range(max(3, args.warmup)):
         step_device()

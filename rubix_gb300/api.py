@@ -54,7 +54,9 @@ class IFURenderer:
 
     def __init__(self, ssp_age, ssp_metallicity, ssp_wavelength, ssp_flux, wave_t, edges,
                  sbin: int, dist_z: float, psf_taps=None, lsf_taps=None, lsf_crop: int = 12,
-                 velocity_axis: int = 2, apply_filter: bool = True, device="cuda"):
+                 velocity_axis: int = 2, apply_filter: bool = True, device="cuda",
+                 noise_s2n: Optional[float] = None, noise_distribution: str = "normal",
+                 noise_seed: int = 0):
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("IFURenderer needs a CUDA device (rubix_gb300 has no CPU path)")
@@ -75,6 +77,9 @@ class IFURenderer:
         self.lsf_crop = int(lsf_crop)
         self.velocity_axis = int(velocity_axis)
         self.apply_filter = bool(apply_filter)
+        self.noise_s2n = None if noise_s2n is None else float(noise_s2n)
+        self.noise_distribution = noise_distribution
+        self.noise_seed = int(noise_seed)
 
     @classmethod
     def from_workload(cls, w, device="cuda", psf=True, lsf=True):
@@ -82,7 +87,7 @@ class IFURenderer:
                    w.sbin, w.dist_z,
                    psf_taps=tel.gaussian_taps_1d(w.psf_size, w.psf_sigma) if psf else None,
                    lsf_taps=tel.lsf_taps(w.lsf_sigma, w.wave_res) if lsf else None,
-                   device=device)
+                   device=device, noise_s2n=getattr(w, "noise_s2n", None))
 
     # -------------------------------------------------------------- steps
     def assign(self, coords):
@@ -111,6 +116,12 @@ class IFURenderer:
     def lsf(self, cube, out=None):
         return ops.lsf_forward(cube, self.lsf_taps, self.lsf_crop, out=out)
 
+    def noise_(self, cube):
+        """apply_noise in place when the renderer has a signal-to-noise (else no-op)."""
+        if self.noise_s2n is not None:
+            ops.apply_noise_(cube, self.noise_s2n, self.noise_distribution, self.noise_seed)
+        return cube
+
     # -------------------------------------------------------------- whole path
     def render(self, coords, velocity, mass, metallicity, age, fuse_lsf=True) -> CubeStages:
         """Whole path.  With ``fuse_lsf`` the LSF runs inside the accumulate kernel and the
@@ -123,8 +134,14 @@ class IFURenderer:
         if fuse:
             c_psf = self.psf(cube) if self.psf_taps is not None else None
             final = c_psf if c_psf is not None else cube
+            if self.noise_s2n is not None and final is cube:
+                final = cube.clone()  # keep the accumulate stage noise-free
+            final = self.noise_(final)
             return CubeStages(idx, mask, perm, offs, cube, c_psf, None, True, final)
         c_psf = self.psf(cube) if self.psf_taps is not None else None
         c_lsf = self.lsf(c_psf if c_psf is not None else cube) if self.lsf_taps is not None else None
         final = c_lsf if c_lsf is not None else (c_psf if c_psf is not None else cube)
+        if self.noise_s2n is not None and final is cube:
+            final = cube.clone()  # keep the accumulate stage noise-free
+        final = self.noise_(final)
         return CubeStages(idx, mask, perm, offs, cube, c_psf, c_lsf, False, final)

@@ -93,10 +93,16 @@ __global__ void __launch_bounds__(kPsfThreads) psf_strip_kernel(PsfArgs a) {
 // wavelength lane and kPsfXB consecutive x positions; the y window of the last M
 // x-convolved rows lives in registers (the row loop is unrolled by M so every window
 // index is static).  Input rows are staged by 4-byte cp.async copies into a ring of
-// kPsfStages shared-memory rows, kPsfStages-1 rows ahead of the row being convolved,
+// S shared-memory rows (up to 8, as many as 48 KB of static shared memory hold),
+// S-1 rows ahead of the row being convolved,
 // so each SM keeps several rows of every strip in flight; one barrier per row.
 constexpr int kPsfXB = 4;
-constexpr int kPsfStages = 4;
+// Ring depth for a tap count M: as many staged rows as fit in 48 KB, at most 8.
+__host__ __device__ constexpr int psf_stages(int M) {
+  return (48 * 1024) / ((kPsfTileX + M - 1) * kPsfTileL * 4) >= 8
+             ? 8
+             : (48 * 1024) / ((kPsfTileX + M - 1) * kPsfTileL * 4);
+}
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
@@ -122,6 +128,8 @@ __device__ __forceinline__ void psf_reg_body(const float* __restrict__ in, float
                                              int by) {
   constexpr int W = kPsfTileX + M - 1;  // staged row width
   constexpr int PER = (W * kPsfTileL + kPsfThreads - 1) / kPsfThreads;
+  constexpr int kPsfStages = psf_stages(M);
+  static_assert(kPsfStages >= 3, "PSF ring needs at least 3 rows");
   __shared__ float s_in[kPsfStages][W * kPsfTileL];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = bx * kPsfTileX;

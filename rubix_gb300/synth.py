@@ -145,7 +145,7 @@ WORKLOADS = {
     "ifu": dict(n=1_000_000, ssp=(221, 6, 1221), fov=30.0, psf_size=15, psf_sigma=1.5, seed=2),
     "diff": dict(n=200_000, ssp=(221, 6, 1221), fov=10.0, psf_size=15, psf_sigma=1.5, seed=3),
     "large": dict(n=10_000_000, ssp=(221, 6, 1221), fov=60.0, psf_size=15, psf_sigma=1.5,
-                  seed=5, bulge_frac=0.3),
+                  seed=5, bulge_frac=0.3, noise_s2n=20.0),
 }
 SPATIAL_RES = 0.2   # arcsec per spaxel (MUSE)
 DIST_Z = 0.1
@@ -168,6 +168,7 @@ class Workload:
     lsf_sigma: float
     wave_res: float
     dist_z: float
+    noise_s2n: float | None = None  # Gaussian noise at this S/N after PSF and LSF
 
 
 def make_workload(name: str, n: int | None = None, edge_cases: bool = True,
@@ -191,4 +192,4 @@ def make_workload(name: str, n: int | None = None, edge_cases: bool = True,
     return Workload(name=name, particles=gal, ssp=ssp, edges=edges, sbin=sbin, wave_t=wave_t,
                     wave_z=tel.cosmological_doppler_shift(DIST_Z, ssp.wavelength),
                     psf_size=cfg["psf_size"], psf_sigma=cfg["psf_sigma"], lsf_sigma=LSF_SIGMA,
-                    wave_res=WAVE_RES, dist_z=DIST_Z)
+                    wave_res=WAVE_RES, dist_z=DIST_Z, noise_s2n=cfg.get("noise_s2n"))
