@@ -151,6 +151,24 @@ __device__ __forceinline__ void adj_build(const AdjArgs& a, const ParticleRec& r
   }
 }
 
+// One-step walk on the two row arrays, branch-free: if x >= e.w advance both entry
+// addresses by one and load both next entries (predicated add and loads).
+__device__ __forceinline__ void walk_step2(float x, unsigned& aa, unsigned& ab, float4& e,
+                                           float4& f) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ge.f32 p, %10, %5;\n\t"
+      "@p add.u32 %0, %0, 16;\n\t"
+      "@p add.u32 %1, %1, 16;\n\t"
+      "@p ld.shared.v4.f32 {%2, %3, %4, %5}, [%0];\n\t"
+      "@p ld.shared.v4.f32 {%6, %7, %8, %9}, [%1];\n\t"
+      "}"
+      : "+r"(aa), "+r"(ab), "+f"(e.x), "+f"(e.y), "+f"(e.z), "+f"(e.w), "+f"(f.x), "+f"(f.y),
+        "+f"(f.z), "+f"(f.w)
+      : "f"(x)
+      : "memory");
+}
+
 // The 8 partial sums of one particle over this thread's R wavelengths.
 template <int R, bool kGeneric>
 __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
@@ -171,6 +189,8 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
     while (k < ke && x >= e.w) { ++k; e = ra[k]; }
   }
   float4 f = rb[k];
+  unsigned aa = static_cast<unsigned>(__cvta_generic_to_shared(ra + k));
+  unsigned ab = static_cast<unsigned>(__cvta_generic_to_shared(rb + k));
 #pragma unroll
   for (int i = 0; i < kAdjSums; ++i) s[i] = 0.f;
 #pragma unroll
@@ -180,10 +200,8 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
       bool moved = false;
       while (k < ke && x >= e.w) { ++k; e = ra[k]; moved = true; }
       if (moved) f = rb[k];
-    } else if (r > 0 && x >= e.w) {
-      ++k;
-      e = ra[k];
-      f = rb[k];
+    } else if (r > 0) {
+      walk_step2(x, aa, ab, e, f);
     }
     const float d = x - e.x;
     const float I = fmaf(d, e.y, e.z);

@@ -211,7 +211,8 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
     float B = (float)(vc / h);
     B = fminf(fmaxf(B, -bmax), bmax);
     const int ks = count_le_scaled(wave_z, n_wave, alpha, t_lo) - 1;
-    int ke = count_le_scaled(wave_z, n_wave, alpha, t_hi) - 1;
+    const int ke_raw = count_le_scaled(wave_z, n_wave, alpha, t_hi) - 1;
+    int ke = ke_raw;
     ke = max(ke, ks);  // keeps the shared-memory row non-empty for any input grid
     const bool coarse = coarse_ok && alpha >= alo && alpha <= ahi;
     // In-range flux sum T: entries ka..kb with t_lo <= lambda'_k <= t_hi, k >= 1.
@@ -219,7 +220,7 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
     if (cell >= 0) {
       int ka = (ks >= 0 && __fmul_rn(wave_z[ks], alpha) >= t_lo) ? ks : ks + 1;
       ka = max(ka, 1);
-      const int kb = min(count_le_scaled(wave_z, n_wave, alpha, t_hi) - 1, n_wave - 1);
+      const int kb = min(ke_raw, n_wave - 1);
       if (ka <= kb) {
         const long long r00 = (long long)(iz - 1) * nA + (ia - 1);
         const long long rr[4] = {r00, r00 + nA, r00 + 1, r00 + nA + 1};  // 00, 10, 01, 11
@@ -390,12 +391,8 @@ inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, const CubeTun
     cube_count_kernel<<<g, 256, 0, st>>>(in.seg_off, in.n_seg, tune.chunk, tune.big_item,
                                          L.slot_cnt, L.big_cnt, L.small_cnt);
     RUBIX_LAUNCH_CHECK("cube_count_kernel");
-    scan_exclusive_1block<<<1, 1024, 0, st>>>(L.slot_cnt, in.n_seg, 1);
-    RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
-    scan_exclusive_1block<<<1, 1024, 0, st>>>(L.big_cnt, in.n_seg, 1);
-    RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
-    scan_exclusive_1block<<<1, 1024, 0, st>>>(L.small_cnt, in.n_seg, 1);
-    RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
+    scan_exclusive_3<<<3, 1024, 0, st>>>(L.slot_cnt, L.big_cnt, L.small_cnt, in.n_seg);
+    RUBIX_LAUNCH_CHECK("scan_exclusive_3");
     cube_fill_items_kernel<<<g, 256, 0, st>>>(in.seg_off, in.n_seg, tune.chunk,
                                               tune.big_item, L.slot_cnt, L.big_cnt,
                                               L.small_cnt, L.items, L.ctrl);

@@ -9,8 +9,22 @@ namespace {
 // Exclusive scan of `count` ints in place by one block of 1024 threads, in tiles of
 // 4096 (4 consecutive values per thread, warp-shuffle scans).  The grand total is
 // written to data[count] when `with_total` is set (data then has count+1 slots).
+__device__ __forceinline__ void scan_exclusive_block(int* __restrict__ data, long long count,
+                                                     int with_total);
+
 __global__ void __launch_bounds__(1024)
 scan_exclusive_1block(int* __restrict__ data, long long count, int with_total) {
+  scan_exclusive_block(data, count, with_total);
+}
+
+// Three independent scans (with totals) in one launch: block b scans array b.
+__global__ void __launch_bounds__(1024)
+scan_exclusive_3(int* __restrict__ a, int* __restrict__ b, int* __restrict__ c, long long count) {
+  scan_exclusive_block(blockIdx.x == 0 ? a : (blockIdx.x == 1 ? b : c), count, 1);
+}
+
+__device__ __forceinline__ void scan_exclusive_block(int* __restrict__ data, long long count,
+                                                     int with_total) {
   __shared__ int s_warp[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   long long carry = 0;

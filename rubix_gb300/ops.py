@@ -163,8 +163,8 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
               _ptr(seg_offsets), int(n_segments), n,
               None if lsf is None else lsf.ctypes.data, 0 if lsf is None else lsf.size,
               int(lsf_crop), _ptr(out), out.stride(0), _ptr(ws), ws.numel(), _stream(dev))
-    # setup, corner table, prefix, count, three scans, fill, main (+ gather when n > 0)
-    _count((9 + (1 if n > 0 else 0)) if n_segments > 0 else 0)
+    # setup, corner table, prefix, count, scans (one launch), fill, main (+ gather)
+    _count((7 + (1 if n > 0 else 0)) if n_segments > 0 else 0)
     if check and n_segments > 0:
         import ctypes
 
@@ -207,8 +207,8 @@ def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, 
               _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
               _ptr(seg_offsets), int(n_segments), n, _ptr(adj), adj.stride(0),
               *[_ptr(g) for g in grads], _ptr(ws), ws.numel(), _stream(dev))
-    # setup, corner table, prefix, count, three scans, fill, adjoint (+ gather when n > 0)
-    _count((9 + (1 if n > 0 else 0)) if (n_segments > 0 and n > 0) else 0)
+    # setup, corner table, prefix, count, scans (one launch), fill, adjoint (+ gather)
+    _count((7 + (1 if n > 0 else 0)) if (n_segments > 0 and n > 0) else 0)
     return tuple(grads)
 
 
