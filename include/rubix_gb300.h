@@ -344,6 +344,27 @@ RUBIX_API int rubix_segmented_dot(const float* a, const float* b, const int64_t*
                                   size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------- */
+/* Galaxy orientation                                                        */
+/* ------------------------------------------------------------------------- */
+/*
+ * rotate_galaxy (rubix/core/rotation.py:11-117, galaxy/alignment.py:66-265):
+ *   rubix_inertia_tensor: out9 (device, float64, row-major 3x3) = the moment-of-inertia
+ *     tensor of the particles with |x| <= halfmass_radius (moment_of_inertia_tensor,
+ *     alignment.py:66-120), including the index padding of rubix's
+ *     jnp.where(..., size=N): particle 0 counts once more for every particle outside.
+ *   rubix_rotate_vectors: out[i] = in[i] . M (row vectors times the host row-major 3x3
+ *     float64 matrix, float64 arithmetic rounded once; in and out may alias).
+ * The caller diagonalises the tensor (eigh, eigenvectors in ascending eigenvalue order)
+ * and composes M = R_inertia . R_euler on the host.
+ */
+RUBIX_API size_t rubix_inertia_workspace_size(void);
+RUBIX_API int rubix_inertia_tensor(const float* positions, int64_t n, int64_t stride,
+                                   const float* masses, float halfmass_radius, double* out9,
+                                   void* workspace, size_t workspace_bytes, void* stream);
+RUBIX_API int rubix_rotate_vectors(const float* in, float* out, int64_t n, int64_t stride_in,
+                                   int64_t stride_out, const double* matrix9, void* stream);
+
+/* ------------------------------------------------------------------------- */
 /* Observation noise                                                         */
 /* ------------------------------------------------------------------------- */
 /*

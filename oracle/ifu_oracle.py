@@ -391,12 +391,15 @@ def particle_spectra(mass, metallicity, age, v_los, ssp_metallicity, ssp_age, ss
 def render_cube(coords, velocity, mass, metallicity, age, edges, sbin,
                 ssp_metallicity, ssp_age, ssp_flux, ssp_wave, dist_z, wave_t,
                 psf_size=None, psf_sigma=None, lsf_sigma=None, wave_res=None,
-                apply_filter=True, velocity_direction="z", chunk=512):
-    """The calc_ifu chain (rubix/config/pipeline_config.yml:1-60) from filter_particles
-    through convolve_lsf, rotation and noise excluded.  Returns a dict of stages."""
+                apply_filter=True, velocity_direction="z", chunk=512, rotation=None):
+    """The calc_ifu chain (rubix/config/pipeline_config.yml:1-60) from rotate_galaxy
+    (when ``rotation`` = (halfmass_radius, alpha, beta, gamma) is given) or
+    filter_particles through convolve_lsf, noise excluded.  Returns a dict of stages."""
     coords = np.asarray(coords, dtype=np.float32)
     velocity = np.asarray(velocity, dtype=np.float32)
     mass = np.asarray(mass, dtype=np.float32)
+    if rotation is not None:
+        coords, velocity = rotate_galaxy(coords, velocity, mass, *rotation)
     metallicity = np.asarray(metallicity, dtype=np.float32)
     age = np.asarray(age, dtype=np.float32)
     edges = np.asarray(edges, dtype=np.float32)
@@ -596,6 +599,61 @@ def lsf_taps_derivative(sigma, wave_res, factor=12):
     S = e.sum()
     t = e / S
     return t, (de - t * de.sum()) / S
+
+
+# ----------------------------------------------------------------------------------
+# Orientation (core/rotation.py:11-117, galaxy/alignment.py:66-265)
+# ----------------------------------------------------------------------------------
+def moment_of_inertia_tensor(positions, masses, halfmass_radius):
+    """alignment.py:66-120 in float64.  The reference selects with
+    ``jnp.where(distances <= r, size=N)``, whose index list is padded with 0: particle 0
+    enters once more for every particle outside the radius."""
+    pos = np.asarray(positions, dtype=np.float32)
+    m = np.asarray(masses, dtype=np.float32).astype(np.float64)
+    d = np.sqrt(np.sum(pos * pos, axis=1, dtype=np.float32))
+    inside = np.nonzero(d <= np.float32(halfmass_radius))[0]
+    idx = np.concatenate([inside, np.zeros(pos.shape[0] - inside.size, dtype=np.int64)])
+    p = pos[idx].astype(np.float64)
+    mm = m[idx]
+    r2 = np.sum(p * p, axis=1)
+    I = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            if i == j:
+                I[i, j] = np.sum(mm * r2 - mm * p[:, i] ** 2)
+            else:
+                I[i, j] = -np.sum(mm * p[:, i] * p[:, j])
+    return I
+
+
+def rotation_matrix_from_inertia_tensor(I):
+    """alignment.py:123-138: eigenvectors as columns, ascending eigenvalues."""
+    w, v = np.linalg.eigh(np.asarray(I, dtype=np.float64))
+    return v[:, np.argsort(w)]
+
+
+def euler_rotation_matrix(alpha, beta, gamma):
+    """alignment.py:162-205: R_z(gamma) R_y(beta) R_x(alpha), degrees."""
+    a, b, g = np.deg2rad([alpha, beta, gamma])
+    Rx = np.array([[1, 0, 0], [0, np.cos(a), -np.sin(a)], [0, np.sin(a), np.cos(a)]])
+    Ry = np.array([[np.cos(b), 0, np.sin(b)], [0, 1, 0], [-np.sin(b), 0, np.cos(b)]])
+    Rz = np.array([[np.cos(g), -np.sin(g), 0], [np.sin(g), np.cos(g), 0], [0, 0, 1]])
+    return Rz @ Ry @ Rx
+
+
+def rotate_galaxy(positions, velocities, masses, halfmass_radius, alpha, beta, gamma):
+    """alignment.py:228-265: principal-frame rotation then Euler rotation, row vectors;
+    float64 products rounded once to float32."""
+    R = rotation_matrix_from_inertia_tensor(
+        moment_of_inertia_tensor(positions, masses, halfmass_radius))
+    M = R @ euler_rotation_matrix(alpha, beta, gamma)
+    pos = (np.asarray(positions, dtype=np.float32).astype(np.float64) @ M).astype(np.float32)
+    vel = (np.asarray(velocities, dtype=np.float32).astype(np.float64) @ M).astype(np.float32)
+    return pos, vel
+
+
+__all__ += ["moment_of_inertia_tensor", "rotation_matrix_from_inertia_tensor",
+            "euler_rotation_matrix", "rotate_galaxy"]
 
 
 # ----------------------------------------------------------------------------------

@@ -14,6 +14,7 @@ from .lsf import get_convolve_lsf  # noqa: F401
 from .noise import get_apply_noise  # noqa: F401
 from .pipeline import RubixPipeline  # noqa: F401
 from .psf import get_convolve_psf  # noqa: F401
+from .rotation import get_galaxy_rotation  # noqa: F401
 from .ssp import get_lookup_interpolation, get_ssp, register_ssp_template  # noqa: F401
 from .telescope import (get_filter_particles, get_spatial_bin_edges,  # noqa: F401
                         get_spaxel_assignment, get_telescope, register_telescope)

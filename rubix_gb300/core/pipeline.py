@@ -1,10 +1,10 @@
 """RubixPipeline (rubix/core/pipeline.py:30-208), eager, on the rubix_gb300 kernels.
 
 Differences from rubix, all outside the particle -> cube path: the particle data is
-passed in (``data=``) instead of being read from simulation files; ``rotate_galaxy``
-expects particles already in the observer frame (it raises if its configuration asks
-for a rotation); the SSP lookup is bilinear (``ssp.method = "linear"``); the noise of
-``apply_noise`` comes from a seeded Philox generator instead of jax.random.
+passed in (``data=``, with ``galaxy.halfmassrad_stars`` for the rotation) instead of
+being read from simulation files; the SSP lookup is bilinear (``ssp.method =
+"linear"``); the noise of ``apply_noise`` comes from a seeded Philox generator instead
+of jax.random.
 """
 
 from __future__ import annotations
@@ -21,22 +21,9 @@ from .ifu import (get_calculate_datacube, get_calculate_spectra,
 from .lsf import get_convolve_lsf
 from .noise import get_apply_noise
 from .psf import get_convolve_psf
+from .rotation import get_galaxy_rotation
 from .ssp import get_ssp
 from .telescope import get_filter_particles, get_spaxel_assignment, get_telescope
-
-
-def get_galaxy_rotation(config: dict):
-    """Particles are taken in the observer frame; a configured rotation is refused."""
-    rot = config.get("galaxy", {}).get("rotation")
-    if rot not in (None, {}, "none") and not (isinstance(rot, dict) and
-                                              all(float(v) == 0 for v in rot.values())):
-        raise NotImplementedError(
-            "galaxy rotation is not part of rubix_gb300: pass particles in the observer frame")
-
-    def rotate_galaxy(rubixdata: RubixData) -> RubixData:
-        return rubixdata
-
-    return rotate_galaxy
 
 
 class RubixPipeline:

@@ -229,6 +229,34 @@ def dot(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def inertia_tensor(coords: torch.Tensor, mass: torch.Tensor, halfmass_radius: float) -> torch.Tensor:
+    """[3, 3] float64 moment-of-inertia tensor of the particles within the radius, with
+    rubix's index padding (particle 0 once more per particle outside)."""
+    coords = _contig("coords", coords, torch.float32)
+    mass = _contig("mass", mass, torch.float32).reshape(-1)
+    c = coords.reshape(-1, coords.shape[-1])
+    out = torch.empty((3, 3), dtype=torch.float64, device=c.device)
+    ws = workspace(_lib.query("rubix_inertia_workspace_size"), c.device)
+    _lib.call("rubix_inertia_tensor", _ptr(c), c.shape[0], c.stride(0), _ptr(mass),
+              float(halfmass_radius), _ptr(out), _ptr(ws), ws.numel(), _stream(c.device))
+    _count(2)
+    return out
+
+
+def rotate_vectors(x: torch.Tensor, matrix, out=None) -> torch.Tensor:
+    """x [..., 3] times the 3x3 float64 matrix (row vectors), float32 result."""
+    x = _contig("x", x, torch.float32)
+    m = np.ascontiguousarray(np.asarray(matrix, dtype=np.float64).reshape(3, 3))
+    rows = x.reshape(-1, 3)
+    if out is None:
+        out = torch.empty_like(rows)
+    o = out.reshape(-1, 3)
+    _lib.call("rubix_rotate_vectors", _ptr(rows), _ptr(o), rows.shape[0], rows.stride(0),
+              o.stride(0), m.ctypes.data, _stream(x.device))
+    _count(1 if rows.shape[0] > 0 else 0)
+    return out.reshape(x.shape)
+
+
 def flux_image(cube: torch.Tensor) -> torch.Tensor:
     """[..., L] -> [...] float32: sum over the last axis (the flux image of a cube)."""
     _check_cuda("cube", cube, torch.float32)

@@ -27,25 +27,39 @@ def _config(w, name="small_test_ssp"):
                       # parity comparison is pre-noise
                       "noise": {"signal_to_noise": 1e30, "noise_distribution": "normal"}},
         "cosmology": {"name": "PLANCK15"},
-        "galaxy": {"dist_z": w.dist_z},
+        "galaxy": {"dist_z": w.dist_z, "rotation": {"type": "face-on"}},
         "ssp": {"template": {"name": name}, "method": "linear"},
     }
 
 
+HALFMASS_RADIUS = 5.0  # kpc, of the synthetic exponential disk (R_d = 3 kpc)
+
+
 def _data(w):
-    from rubix_gb300.core import RubixData, StarsData
+    from rubix_gb300.core import Galaxy, RubixData, StarsData
 
     p = w.particles
-    return RubixData(stars=StarsData(coords=p.coords.copy(), velocity=p.velocity.copy(),
+    return RubixData(galaxy=Galaxy(halfmassrad_stars=HALFMASS_RADIUS),
+                     stars=StarsData(coords=p.coords.copy(), velocity=p.velocity.copy(),
                                      mass=p.mass.copy(), metallicity=p.metallicity.copy(),
                                      age=p.age.copy()))
+
+
+def _oracle_pipeline(w):
+    """The oracle's calc_ifu chain with the face-on rotation of the step configs."""
+    p = w.particles
+    return oracle.render_cube(p.coords, p.velocity, p.mass, p.metallicity, p.age, w.edges,
+                              w.sbin, w.ssp.metallicity, w.ssp.age, w.ssp.flux,
+                              w.ssp.wavelength, w.dist_z, w.wave_t, psf_size=w.psf_size,
+                              psf_sigma=w.psf_sigma, lsf_sigma=w.lsf_sigma, wave_res=w.wave_res,
+                              rotation=(HALFMASS_RADIUS, 0.0, 0.0, 0.0))
 
 
 def test_rubix_pipeline_matches_oracle():
     from rubix_gb300.core import RubixPipeline
 
     w = workload("small")
-    ref = oracle_stages("small")
+    ref = _oracle_pipeline(w)
     out = RubixPipeline(_config(w), _data(w)).run()
     cube = out.stars.datacube.cpu().numpy()
     assert cube.shape == (25, 25, 3721)
@@ -61,7 +75,7 @@ def test_rubix_pipeline_noise():
 
     w = workload("small")
     cfg = _config(w)
-    ref = oracle_stages("small")["final"]
+    ref = _oracle_pipeline(w)["final"]
     cfg["telescope"]["noise"] = {"signal_to_noise": 20, "noise_distribution": "normal"}
     out = RubixPipeline(cfg, _data(w)).run().stars.datacube.cpu().numpy().astype(np.float64)
     sig, med = oracle.noise_sigma(ref, 20.0)
