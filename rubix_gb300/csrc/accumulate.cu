@@ -14,8 +14,9 @@
 //     persistent kernel from an atomic counter.  A block of 384 threads owns the
 //     telescope grid of its spaxel: thread i holds R consecutive wavelengths
 //     t = i*R + r in registers (wavelength, bin width, accumulator).
-//   * Per batch of kPB particles one thread issues a 1-D TMA bulk copy of each
-//     particle's corner-table segment (its bracket range only) into shared memory; it
+//   * A batch is 1-3 particles packed by their bracket lengths into staging and row
+//     pools of kPB * (nW + 2) entries.  One thread issues a 1-D TMA bulk copy of each
+//     particle's corner-table segment (its bracket range only) into the staging pool; it
 //     completes on an mbarrier while the block evaluates the previous batch.  The block
 //     then builds per particle the row of entries (lambda'_k, slope_k, G_k,
 //     lambda'_{k+1}) of the mixed template G = sum_c w_c F_c; the in-range flux sum T
@@ -23,7 +24,7 @@
 //   * Evaluation: each thread finds the exact bracket of its first wavelength (bucket
 //     table + exact comparisons on lambda') and walks forward over its R wavelengths;
 //     when every SSP interval is wider than every telescope bin the walk advances at
-//     most once per wavelength (one predicated load); the two particles of a batch are
+//     most once per wavelength (one predicated load); the particles of a batch are
 //     evaluated interleaved for instruction-level parallelism.  Interpolated values stay in
 //     registers while T' = sum_t I_t dlambda_t is reduced over the block; then
 //     s = nan_to_num(T/T') and the accumulators take mass * s * I.
@@ -62,7 +63,8 @@ struct MainArgs {
 };
 
 // Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned): the TMA
-// staging of a batch's corner segments [kPB][row_cap] and its rows [kPB][row_cap].
+// staging pool and the row pool, P = kPB * row_cap entries each, shared by the up to
+// kPBMax particles of a batch.
 struct SmemLayout {
   size_t wz, bucket, stage, rows, red, rec, total;
 };
@@ -77,39 +79,71 @@ __host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
   L.rows = o;   // also holds the zero-padded spectrum of the LSF epilogue
   o = al(o + std::max(sizeof(float4) * kPB * (size_t)row_cap,
                       sizeof(float) * (size_t)(kMaxWaveT + 2 * kMaxLsfTaps + 8)));
-  L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 2);
+  L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 4);
   L.rec = o;    o = al(o + sizeof(ParticleRec) * kMaxChunk);
   L.total = o;
   return L;
 }
 
-// Thread 0: arm the barrier and issue one bulk copy per particle of the batch: the
-// corner-table entries k in [max(kstart,0), min(kend+1, nW-1)] of its cell.
-__device__ __forceinline__ void issue_stage(const MainArgs& a, const ParticleRec* recs, int cnt,
-                                            float4* stage, uint64_t* bar) {
-  fence_proxy_async_smem();  // earlier generic reads of the staging buffer come first
-  uint32_t bytes = 0;
-  int klo[kPB], nk[kPB], cells[kPB];
+// Batches of up to kPBMax particles packed into the staging and row pools of P entries
+// each: particle j of a batch takes n_e + 2 entries (its row, and its staged corner
+// segment of at most n_e + 1 entries) at the same offset in both pools.  Every thread
+// derives the same plan from the records.
+constexpr int kPBMax = 3;
+
+struct BatchPlan {
+  int cnt;
+  int off[kPBMax];
+};
+
+__device__ __forceinline__ int rec_ne(const ParticleRec& r) {
+  return (r.b.z & ~kGenericFlag) - r.b.y + 1;
+}
+
+__device__ __forceinline__ BatchPlan plan_batch(const ParticleRec* recs, int left, int P) {
+  BatchPlan b;
+  b.cnt = left > 0 ? 1 : 0;
+  b.off[0] = 0;
+  b.off[1] = b.off[2] = 0;
+  if (left <= 0) return b;
+  int used = rec_ne(recs[0]) + 2;
 #pragma unroll
-  for (int p = 0; p < kPB; ++p) {
-    cells[p] = -1;
-    klo[p] = 0;
-    nk[p] = 0;
-    if (p < cnt) {
-      const int4 b = recs[p].b;
-      const int ks = b.y, ke = b.z & ~kGenericFlag;
-      klo[p] = max(ks, 0);
-      nk[p] = min(ke + 1, a.n_wave - 1) - klo[p] + 1;
-      cells[p] = b.x;
-      if (b.x >= 0) bytes += 16u * (uint32_t)nk[p];
+  for (int j = 1; j < kPBMax; ++j) {
+    if (j >= left) break;
+    const int need = rec_ne(recs[j]) + 2;
+    if (used + need > P) break;
+    b.off[j] = used;
+    used += need;
+    b.cnt = j + 1;
+  }
+  return b;
+}
+
+// Thread 0: arm the barrier and issue one bulk copy per particle of a planned batch: the
+// corner-table entries k in [max(kstart,0), min(kend+1, nW-1)] of its cell.
+__device__ __forceinline__ void issue_plan(const MainArgs& a, const ParticleRec* recs,
+                                           const BatchPlan& bp, float4* stage, uint64_t* bar) {
+  fence_proxy_async_smem();
+  uint32_t bytes = 0;
+#pragma unroll
+  for (int p = 0; p < kPBMax; ++p) {
+    if (p < bp.cnt && recs[p].b.x >= 0) {
+      const int ks = recs[p].b.y, ke = recs[p].b.z & ~kGenericFlag;
+      const int klo = max(ks, 0);
+      bytes += 16u * (uint32_t)(min(ke + 1, a.n_wave - 1) - klo + 1);
     }
   }
   mbar_arrive_expect_tx(bar, bytes);
 #pragma unroll
-  for (int p = 0; p < kPB; ++p)
-    if (cells[p] >= 0)
-      bulk_copy_g2s(stage + (size_t)p * a.row_cap, a.ct + (long long)cells[p] * a.n_wave + klo[p],
-                    16u * nk[p], bar);
+  for (int p = 0; p < kPBMax; ++p) {
+    if (p < bp.cnt && recs[p].b.x >= 0) {
+      const int ks = recs[p].b.y, ke = recs[p].b.z & ~kGenericFlag;
+      const int klo = max(ks, 0);
+      const int nk = min(ke + 1, a.n_wave - 1) - klo + 1;
+      bulk_copy_g2s(stage + bp.off[p], a.ct + (long long)recs[p].b.x * a.n_wave + klo,
+                    16u * nk, bar);
+    }
+  }
 }
 
 struct RowParams {
@@ -228,28 +262,88 @@ __device__ __forceinline__ void build_step_pair(const RowParams& q0, const RowPa
   }
 }
 
-// Builds the rows of the (one or two) particles of a batch into `rows`
-// ([kPB][row_cap]) from the staged corners, interleaving their steps.
-__device__ __forceinline__ void build_rows(const MainArgs& a, const ParticleRec* recs, int cnt,
-                                           const float* __restrict__ s_wz,
+// Two interior steps of one particle at two bases, interleaved.
+__device__ __forceinline__ void build_step_pair2(const RowParams& q, int b0, int b1,
+                                                 const float* __restrict__ s_wz, int lane) {
+  const int e0 = b0 + lane, e1 = b1 + lane;
+  const int k0 = q.ks + e0, k1 = q.ks + e1;
+  const float4 c0 = q.st[k0];
+  const float4 c1 = q.st[k1];
+  const float z0 = s_wz[k0], z1 = s_wz[k1];
+  float G0 = q.w00 * c0.x, G1 = q.w00 * c1.x;
+  G0 = fmaf(q.w10, c0.y, G0);
+  G1 = fmaf(q.w10, c1.y, G1);
+  G0 = fmaf(q.w01, c0.z, G0);
+  G1 = fmaf(q.w01, c1.z, G1);
+  G0 = fmaf(q.w11, c0.w, G0);
+  G1 = fmaf(q.w11, c1.w, G1);
+  if (!q.has_cell) {
+    G0 = 0.f;
+    G1 = 0.f;
+  }
+  const float lp0 = __fmul_rn(z0, q.alpha), lp1 = __fmul_rn(z1, q.alpha);
+  const float lpn0 = __shfl_down_sync(0xffffffffu, lp0, 1);
+  const float lpn1 = __shfl_down_sync(0xffffffffu, lp1, 1);
+  const float Gn0 = __shfl_down_sync(0xffffffffu, G0, 1);
+  const float Gn1 = __shfl_down_sync(0xffffffffu, G1, 1);
+  if (lane < 31) {
+    const float dl0 = lpn0 - lp0, dl1 = lpn1 - lp1;
+    const float sl0 = dl0 > 0.f ? __fdividef(Gn0 - G0, dl0) : 0.f;
+    const float sl1 = dl1 > 0.f ? __fdividef(Gn1 - G1, dl1) : 0.f;
+    q.row[e0] = make_float4(lp0, sl0, G0, lpn0);
+    q.row[e1] = make_float4(lp1, sl1, G1, lpn1);
+  }
+}
+
+// Builds the rows of a planned batch (1..3 particles) from the staged corners: the
+// first two particles' 31-entry steps interleaved, the third's interleaved with its
+// own next step.
+__device__ __forceinline__ void build_plan(const MainArgs& a, const ParticleRec* recs,
+                                           const BatchPlan& bp, const float* __restrict__ s_wz,
                                            const float4* __restrict__ stage,
                                            float4* __restrict__ rows, int lane, int warp) {
   const RowParams q0 = row_params(recs[0], a, stage, rows);
-  if (cnt > 1) {
-    const RowParams q1 = row_params(recs[1], a, stage + a.row_cap, rows + a.row_cap);
-    const int n_max = max(q0.n_e, q1.n_e);
-    for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
-      if (base < q0.n_e && base < q1.n_e && interior(q0, base) && interior(q1, base)) {
-        build_step_pair(q0, q1, base, s_wz, lane);
-      } else {
-        if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
-        if (base < q1.n_e) build_step(q1, base, a.n_wave, s_wz, lane);
-      }
-    }
-  } else {
+  if (bp.cnt == 1) {
     for (int base = warp * 31; base < q0.n_e; base += kAccWarps * 31)
       build_step(q0, base, a.n_wave, s_wz, lane);
+    return;
   }
+  const RowParams q1 = row_params(recs[1], a, stage + bp.off[1], rows + bp.off[1]);
+  const int n_max = max(q0.n_e, q1.n_e);
+  for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
+    if (base < q0.n_e && base < q1.n_e && interior(q0, base) && interior(q1, base)) {
+      build_step_pair(q0, q1, base, s_wz, lane);
+    } else {
+      if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
+      if (base < q1.n_e) build_step(q1, base, a.n_wave, s_wz, lane);
+    }
+  }
+  if (bp.cnt == 3) {
+    const RowParams q2 = row_params(recs[2], a, stage + bp.off[2], rows + bp.off[2]);
+    for (int base = warp * 31; base < q2.n_e; base += 2 * kAccWarps * 31) {
+      const int b2 = base + kAccWarps * 31;
+      if (b2 < q2.n_e && interior(q2, base) && interior(q2, b2)) {
+        build_step_pair2(q2, base, b2, s_wz, lane);
+      } else {
+        build_step(q2, base, a.n_wave, s_wz, lane);
+        if (b2 < q2.n_e) build_step(q2, b2, a.n_wave, s_wz, lane);
+      }
+    }
+  }
+}
+
+// Sums 4 values over the 32 lanes with 6 shuffles; lane 0 ends with the total of v0,
+// lane 8 with v1, lane 16 with v2, lane 24 with v3.
+__device__ __forceinline__ float warp_reduce4(float v0, float v1, float v2, float v3, int lane) {
+  const bool b4 = lane & 16;
+  const float a0 = (b4 ? v2 : v0) + __shfl_xor_sync(0xffffffffu, b4 ? v0 : v2, 16);
+  const float a1 = (b4 ? v3 : v1) + __shfl_xor_sync(0xffffffffu, b4 ? v1 : v3, 16);
+  const bool b3 = lane & 8;
+  float c = (b3 ? a1 : a0) + __shfl_xor_sync(0xffffffffu, b3 ? a0 : a1, 8);
+  c += __shfl_xor_sync(0xffffffffu, c, 4);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  return c;
 }
 
 // Sums 2 values over the 32 lanes with 5 shuffles; lane 0 ends with the total of v0,
@@ -303,7 +397,7 @@ template <int R, bool kGeneric>
 __device__ __forceinline__ float eval_particle(const float4* __restrict__ rowp, int ks, int ke,
                                                float B, float A0,
                                                const int2* __restrict__ s_bucket,
-                                               const float (&lam)[R], const float (&dlam)[R],
+                                               const float (&lam)[R], float lam_prev,
                                                float (&I)[R]) {
   float4 e;
   int k = first_bracket(rowp, ks, ke, B, A0, s_bucket, lam[0], e);
@@ -319,7 +413,7 @@ __device__ __forceinline__ float eval_particle(const float4* __restrict__ rowp, 
     }
     const float v = fmaf(x - e.x, e.y, e.z);
     I[r] = v;
-    tp = fmaf(v, dlam[r], tp);
+    tp = fmaf(v, x - (r > 0 ? lam[r - 1] : lam_prev), tp);
   }
   return tp;
 }
@@ -331,7 +425,7 @@ __device__ __forceinline__ void eval_pair(const float4* __restrict__ row0, int k
                                           float B0, const float4* __restrict__ row1, int ks1,
                                           int ke1, float B1, float A0,
                                           const int2* __restrict__ s_bucket,
-                                          const float (&lam)[R], const float (&dlam)[R],
+                                          const float (&lam)[R], float lam_prev,
                                           float (&I0)[R], float (&I1)[R], float& tp0,
                                           float& tp1) {
   float4 e0, e1;
@@ -350,10 +444,51 @@ __device__ __forceinline__ void eval_pair(const float4* __restrict__ row0, int k
     }
     const float v0 = fmaf(x - e0.x, e0.y, e0.z);
     const float v1 = fmaf(x - e1.x, e1.y, e1.z);
+    const float d = x - (r > 0 ? lam[r - 1] : lam_prev);
     I0[r] = v0;
     I1[r] = v1;
-    tp0 = fmaf(v0, dlam[r], tp0);
-    tp1 = fmaf(v1, dlam[r], tp1);
+    tp0 = fmaf(v0, d, tp0);
+    tp1 = fmaf(v1, d, tp1);
+  }
+}
+
+// Three particles on the one-step walk, interleaved; dlambda_t recomputed from the
+// wavelengths (lam_prev = the wavelength before this thread's first one).
+template <int R>
+__device__ __forceinline__ void eval_triple(const float4* __restrict__ row0, int ks0, int ke0,
+                                            float B0, const float4* __restrict__ row1, int ks1,
+                                            int ke1, float B1, const float4* __restrict__ row2,
+                                            int ks2, int ke2, float B2, float A0,
+                                            const int2* __restrict__ s_bucket,
+                                            const float (&lam)[R], float lam_prev,
+                                            float (&I0)[R], float (&I1)[R], float (&I2)[R],
+                                            float& tp0, float& tp1, float& tp2) {
+  float4 e0, e1, e2;
+  const int k0 = first_bracket(row0, ks0, ke0, B0, A0, s_bucket, lam[0], e0);
+  const int k1 = first_bracket(row1, ks1, ke1, B1, A0, s_bucket, lam[0], e1);
+  const int k2 = first_bracket(row2, ks2, ke2, B2, A0, s_bucket, lam[0], e2);
+  unsigned a0 = static_cast<unsigned>(__cvta_generic_to_shared(row0 + k0));
+  unsigned a1 = static_cast<unsigned>(__cvta_generic_to_shared(row1 + k1));
+  unsigned a2 = static_cast<unsigned>(__cvta_generic_to_shared(row2 + k2));
+  tp0 = tp1 = tp2 = 0.f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float x = lam[r];
+    const float d = x - (r > 0 ? lam[r - 1] : lam_prev);
+    if (r > 0) {
+      walk_step(x, a0, e0);
+      walk_step(x, a1, e1);
+      walk_step(x, a2, e2);
+    }
+    const float v0 = fmaf(x - e0.x, e0.y, e0.z);
+    const float v1 = fmaf(x - e1.x, e1.y, e1.z);
+    const float v2 = fmaf(x - e2.x, e2.y, e2.z);
+    I0[r] = v0;
+    I1[r] = v1;
+    I2[r] = v2;
+    tp0 = fmaf(v0, d, tp0);
+    tp1 = fmaf(v1, d, tp1);
+    tp2 = fmaf(v2, d, tp2);
   }
 }
 
@@ -396,9 +531,9 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   const SmemLayout SL = smem_layout(a.n_wave, a.row_cap);
   float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
   int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
-  float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);      // [kPB][row_cap]
-  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);        // [kPB][row_cap]
-  float* s_red = reinterpret_cast<float*>(smem + SL.red);            // [2][warps][2]
+  float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);      // pool of P entries
+  float4* s_rows = reinterpret_cast<float4*>(smem + SL.rows);        // pool of P entries
+  float* s_red = reinterpret_cast<float*>(smem + SL.red);            // [2][warps][4]
   ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);  // records of the item
   float* s_spec = reinterpret_cast<float*>(s_rows);  // LSF epilogue reuses the rows
   __shared__ uint64_t s_bar;
@@ -415,17 +550,19 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
 
   const int n_t = a.n_t;
   const int t0 = tid * R;
-  float lam[R], dlam[R], acc[R];
+  const int P = kPB * a.row_cap;
+  float lam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int t = t0 + r;
-    const int tc = t < n_t ? t : n_t - 1;
-    lam[r] = a.wave_t[tc];
-    dlam[r] = (t < n_t && t > 0) ? (a.wave_t[t] - a.wave_t[t - 1]) : 0.f;
+    lam[r] = a.wave_t[t < n_t ? t : n_t - 1];
   }
+  // wavelength before the first one (dlambda_0 = 0: rubix's prepend-diff)
+  const float lam_prev = a.wave_t[t0 == 0 ? 0 : min(t0 - 1, n_t - 1)];
   const float A0 = a.At[t0 < n_t ? t0 : n_t - 1];
   const int n_items = a.ctrl->n_items;
   uint32_t phase = 0;
+  int step = 0;
   __syncthreads();
 
   for (;;) {
@@ -440,24 +577,24 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
     const long long jb = (long long)seg_b + (long long)chunk * a.chunk;
     const long long je = min((long long)seg_e, jb + a.chunk);
     const int np = (int)(je - jb);
-    const int nbatch = (np + kPB - 1) / kPB;
 
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = 0.f;
     // records of this item into shared memory (one 48-byte record per thread)
     for (int i = tid; i < np; i += kAccThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
-    if (nbatch > 0 && tid == 0) issue_stage(a, s_rec, min(kPB, np), s_stage, &s_bar);
+    BatchPlan bp = plan_batch(s_rec, np, P);
+    if (np > 0 && tid == 0) issue_plan(a, s_rec, bp, s_stage, &s_bar);
 
-    // Batch bt: wait for its staged corners, build its rows, issue the next batch's
-    // copies, evaluate, reduce T'.
-    for (int bt = 0; bt < nbatch; ++bt) {
-      const int buf = bt & 1;
-      const int cnt = min(kPB, np - bt * kPB);
-      const ParticleRec* recs = s_rec + bt * kPB;
+    // Batch at p0: wait for its staged corners, build its rows, stage the next batch,
+    // evaluate, reduce T'.
+    for (int p0 = 0; p0 < np; ++step) {
+      const int buf = step & 1;
+      const int cnt = bp.cnt;
+      const ParticleRec* recs = s_rec + p0;
       if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
       phase ^= 1u;
-      build_rows(a, recs, cnt, s_wz, s_stage, s_rows, lane, warp);
+      build_plan(a, recs, bp, s_wz, s_stage, s_rows, lane, warp);
       __syncthreads();  // rows ready; staging consumed
       if (s_fail) {
         if (tid == 0) {
@@ -466,69 +603,75 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
         }
         return;
       }
-      if (bt + 1 < nbatch && tid == 0)
-        issue_stage(a, recs + kPB, min(kPB, np - (bt + 1) * kPB), s_stage, &s_bar);
-      const float4* rows = s_rows;
-      float I[kPB][R];
-      float tp[kPB];
-      const float B0 = recs[0].a.z;
+      const int p1 = p0 + cnt;
+      const BatchPlan bn = plan_batch(s_rec + p1, np - p1, P);
+      if (p1 < np && tid == 0) issue_plan(a, s_rec + p1, bn, s_stage, &s_bar);
+
+      float I[kPBMax][R];
+      float tp[kPBMax];
       const int4 rb0 = recs[0].b;
-      const int ks0 = rb0.y, ke0 = rb0.z & ~kGenericFlag;
-      if (cnt > 1) {
-        const float B1 = recs[1].a.z;
-        const int4 rb1 = recs[1].b;
-        const int ks1 = rb1.y, ke1 = rb1.z & ~kGenericFlag;
-        if (!((rb0.z | rb1.z) & kGenericFlag)) {
-          eval_pair<R>(rows - ks0, ks0, ke0, B0, rows + a.row_cap - ks1, ks1, ke1, B1, A0,
-                       s_bucket, lam, dlam, I[0], I[1], tp[0], tp[1]);
-        } else {
-          tp[0] = (rb0.z & kGenericFlag)
-                      ? eval_particle<R, true>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam, dlam,
-                                               I[0])
-                      : eval_particle<R, false>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam,
-                                                dlam, I[0]);
-          tp[1] = (rb1.z & kGenericFlag)
-                      ? eval_particle<R, true>(rows + a.row_cap - ks1, ks1, ke1, B1, A0,
-                                               s_bucket, lam, dlam, I[1])
-                      : eval_particle<R, false>(rows + a.row_cap - ks1, ks1, ke1, B1, A0,
-                                                s_bucket, lam, dlam, I[1]);
-        }
-      } else {
-        tp[0] = (rb0.z & kGenericFlag)
-                    ? eval_particle<R, true>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam, dlam,
-                                             I[0])
-                    : eval_particle<R, false>(rows - ks0, ks0, ke0, B0, A0, s_bucket, lam, dlam,
-                                              I[0]);
-        tp[1] = 0.f;
+      const int4 rb1 = cnt > 1 ? recs[1].b : rb0;
+      const int4 rb2 = cnt > 2 ? recs[2].b : rb0;
+      const bool generic = ((rb0.z | rb1.z | rb2.z) & kGenericFlag) != 0;
+      const float4* row0 = s_rows - rb0.y;
+      const float4* row1 = s_rows + bp.off[1] - rb1.y;
+      const float4* row2 = s_rows + bp.off[2] - rb2.y;
+      if (cnt == 3 && !generic) {
+        eval_triple<R>(row0, rb0.y, rb0.z, recs[0].a.z, row1, rb1.y, rb1.z, recs[1].a.z, row2,
+                       rb2.y, rb2.z, recs[2].a.z, A0, s_bucket, lam, lam_prev, I[0], I[1], I[2],
+                       tp[0], tp[1], tp[2]);
+      } else if (cnt == 2 && !generic) {
+        eval_pair<R>(row0, rb0.y, rb0.z, recs[0].a.z, row1, rb1.y, rb1.z, recs[1].a.z, A0,
+                     s_bucket, lam, lam_prev, I[0], I[1], tp[0], tp[1]);
+        tp[2] = 0.f;
 #pragma unroll
-        for (int r = 0; r < R; ++r) I[1][r] = 0.f;
+        for (int r = 0; r < R; ++r) I[2][r] = 0.f;
+      } else {
+#pragma unroll
+        for (int p = 0; p < kPBMax; ++p) {
+          tp[p] = 0.f;
+#pragma unroll
+          for (int r = 0; r < R; ++r) I[p][r] = 0.f;
+          if (p < cnt) {
+            const int4 rb = recs[p].b;
+            const int ke = rb.z & ~kGenericFlag;
+            const float4* rowp = s_rows + bp.off[p] - rb.y;
+            tp[p] = (rb.z & kGenericFlag)
+                        ? eval_particle<R, true>(rowp, rb.y, ke, recs[p].a.z, A0, s_bucket, lam,
+                                                 lam_prev, I[p])
+                        : eval_particle<R, false>(rowp, rb.y, ke, recs[p].a.z, A0, s_bucket,
+                                                  lam, lam_prev, I[p]);
+          }
+        }
       }
-      // T'0, T'1 over the warp, then over the block (fixed order: deterministic).
-      const float wsum = warp_reduce2(tp[0], tp[1], lane);
-      if ((lane & 15) == 0) s_red[(buf * kAccWarps + warp) * 2 + (lane >> 4)] = wsum;
-      __syncthreads();  // partial sums of batch bt ready; rows free for the next build
-      // lanes 0..15 take warp (lane & 15)'s partial of T'0, lanes 16..31 of T'1
-      const int wl = lane & 15;
-      float v = (wl < kAccWarps) ? s_red[(buf * kAccWarps + wl) * 2 + (lane >> 4)] : 0.f;
-      v += __shfl_xor_sync(0xffffffffu, v, 8);
+      // T'0..T'2 over the warp, then over the block (fixed order: deterministic).
+      const float wsum = warp_reduce4(tp[0], tp[1], tp[2], 0.f, lane);
+      if ((lane & 7) == 0) s_red[(buf * kAccWarps + warp) * 4 + (lane >> 3)] = wsum;
+      __syncthreads();
+      // lane l: value p = l >> 3 of warps (l & 7) and (l & 7) + 8
+      const int pv = lane >> 3, w0 = lane & 7;
+      float v = s_red[(buf * kAccWarps + w0) * 4 + pv];
+      if (w0 + 8 < kAccWarps) v += s_red[(buf * kAccWarps + w0 + 8) * 4 + pv];
       v += __shfl_xor_sync(0xffffffffu, v, 4);
       v += __shfl_xor_sync(0xffffffffu, v, 2);
       v += __shfl_xor_sync(0xffffffffu, v, 1);
-      // lane 0: T'0, lane 16: T'1
+      // lanes 0, 8, 16: T'0, T'1, T'2
       float beta_l = 0.f;
-      if (lane == 0 || lane == 16) {
-        const int p = lane >> 4;
-        const float4 ra = recs[p].a, rc = recs[p].c;  // lane-dependent index: shared memory
+      if ((lane & 7) == 0 && pv < cnt) {
+        const float4 ra = recs[pv].a, rc = recs[pv].c;  // lane-dependent index: shared memory
         float sc = rc.x / v;
         if (sc != sc) sc = 0.f;
         if (isinf(sc)) sc = copysignf(kFltMax, sc);
-        const float m = ra.x;
-        beta_l = (p < cnt && m != 0.f) ? m * sc : 0.f;
+        beta_l = ra.x != 0.f ? ra.x * sc : 0.f;
       }
       const float beta0 = __shfl_sync(0xffffffffu, beta_l, 0);
-      const float beta1 = __shfl_sync(0xffffffffu, beta_l, 16);
+      const float beta1 = __shfl_sync(0xffffffffu, beta_l, 8);
+      const float beta2 = __shfl_sync(0xffffffffu, beta_l, 16);
 #pragma unroll
-      for (int r = 0; r < R; ++r) acc[r] = fmaf(beta1, I[1][r], fmaf(beta0, I[0][r], acc[r]));
+      for (int r = 0; r < R; ++r)
+        acc[r] = fmaf(beta2, I[2][r], fmaf(beta1, I[1][r], fmaf(beta0, I[0][r], acc[r])));
+      p0 = p1;
+      bp = bn;
     }
 
     const int nch = cnt_s <= a.chunk ? 1 : (cnt_s + a.chunk - 1) / a.chunk;
@@ -567,7 +710,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       if (a.lsf_k > 0) {
         __syncthreads();  // rows free (last batch evaluated) before reuse as spectrum
         const int lead = a.lsf_k - 1 - a.lsf_crop;
-        // zero padding: [0, lead) and [lead + n_t, lead + R*256 + K)
+        // zero padding: [0, lead) and [lead + n_t, lead + R*384 + K)
         for (int i = tid; i < lead; i += kAccThreads) s_spec[i] = 0.f;
         for (int i = lead + n_t + tid; i < lead + kAccThreads * R + a.lsf_k; i += kAccThreads)
           s_spec[i] = 0.f;

@@ -21,7 +21,7 @@ namespace {
 
 constexpr int kAccThreads = 384;  // forward kernel: 2 blocks of 12 warps per SM
 constexpr int kAccWarps = kAccThreads / 32;
-constexpr int kPB = 2;          // particles per batch (the block reduction packs 2x2 values)
+constexpr int kPB = 2;          // staging/row pools of the forward kernel: kPB full rows
 constexpr int kMaxChunk = 256;  // largest work item (particles); records staged per item
 constexpr int kMinChunk = 32;
 constexpr int kBuckets = 1024;  // log-wavelength bucket table entries
