@@ -143,6 +143,78 @@ RUBIX_API int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity
 RUBIX_API int rubix_cube_status(const void* workspace, int* device_error, void* stream);
 
 /*
+ * Replaces, in the dusty pipeline (rubix/config/pipeline_config.yml:97-111), the
+ * extinction factor that calculate_extinction (rubix/core/dust.py:53-63 ->
+ * rubix/spectra/dust/dust_extinction.py:345-358) multiplies into every resampled
+ * spectrum before calculate_datacube sums them.
+ *
+ * rubix_cube_fwd with every particle's resampled spectrum multiplied by its dust
+ * transmission 2^(ext_exponent[t] * av[i]) = 10^(-0.4 A(lambda_t)/A(V) * A_V,i) before
+ * the per-spaxel sum.  av[i]: A_V of particle i (input order, rubix_dust_av);
+ * ext_exponent[t] = -0.4 * log2(10) * A(lambda_t)/A(V) of the extinction model at the
+ * telescope wavelengths (n_wave_t floats).  Same workspace (rubix_cube_workspace_size),
+ * limits, determinism and status word as rubix_cube_fwd.
+ */
+RUBIX_API int rubix_cube_fwd_dust(const float* ssp_flux, const float* ssp_metallicity,
+                                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                                  int32_t n_age, int32_t n_wave, const float* wave_t,
+                                  int32_t n_wave_t, const float* mass, const float* metallicity,
+                                  const float* age, const float* velocity, int64_t vel_stride,
+                                  int32_t vel_component, const float* av,
+                                  const float* ext_exponent, const int32_t* perm,
+                                  const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                  const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
+                                  float* cube, int64_t spaxel_stride, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/*
+ * Replaces the per-cell extinction of rubix/spectra/dust/dust_extinction.py:291-306
+ * (12 + log10(O/(16 H)), calculate_dust_to_gas_ratio :13-90, calculate_extinction
+ * :93-160, divided by the spaxel area).
+ *
+ * ext_out[i] = mass[i] * DGR(g_i) * scale / spaxel_area with
+ * g_i = 12 + log10(metals[i*metals_stride + o_col] / (16 * metals[i*metals_stride + h_col]))
+ * and DGR(g) = 1 / 10^(a + alpha * (x_sol - g)); dgr_params = {x_sol, a_hi, alpha_hi,
+ * a_lo, alpha_lo, x_transition}: with broken != 0 the (a_lo, alpha_lo) branch applies
+ * where g <= x_transition (Remy-Ruyer et al. 2014 broken power law), else (a_hi,
+ * alpha_hi) everywhere.  scale = 3 pi (Msun/kpc^2 in g/cm^2) / (0.4 ln10 lambda_V rho_D).
+ */
+RUBIX_API int rubix_dust_gas_extinction(const float* mass, const float* metals,
+                                        int64_t metals_stride, int32_t h_col, int32_t o_col,
+                                        int64_t n, const float* dgr_params, int32_t broken,
+                                        float scale, float spaxel_area, float* ext_out,
+                                        void* stream);
+
+/*
+ * Replaces the column-density part of apply_spaxel_extinction
+ * (rubix/spectra/dust/dust_extinction.py:262-343): the A_V of every star.
+ *
+ * Gas cell j: z = gas_coords[j*gas_stride + 2], pixel assignment gas_pa[j], extinction
+ * gas_ext[j] (rubix_dust_gas_extinction); star i likewise (star_coords, star_pa).
+ * Spaxel of a cell or star: min(pa, n_segments - 1); pa_limit bounds every assignment
+ * (pa < pa_limit; (n_edges-1)^2 of the spaxel assignment).  av_out[i] is rubix's value:
+ * jnp.interp of the star's z, extrapolating on the left, over its spaxel's cells
+ * (z, cumulative extinction in (assignment, z) order) merged with every other cell at
+ * (fl32(z * 1e30), 0) in rubix's stable-sort order.  No gas (n_gas = 0) gives 0.
+ * Deterministic; about 40 launches; no allocation.
+ */
+/*
+ * Replaces rubix/spectra/dust/dust_extinction.py:345-358 on materialised spectra
+ * (rubixdata.stars.spectra * extinction): rows[i*row_stride + t] *=
+ * 2^(ext_exponent[t] * av[i]) for i < n, t < n_wave_t.
+ */
+RUBIX_API int rubix_dust_apply_rows(float* rows, int64_t n, int32_t n_wave_t,
+                                    int64_t row_stride, const float* av,
+                                    const float* ext_exponent, void* stream);
+
+RUBIX_API size_t rubix_dust_av_workspace_size(int64_t n_gas, int32_t n_segments);
+RUBIX_API int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const int32_t* gas_pa,
+                            const float* gas_ext, int64_t n_gas, const float* star_coords,
+                            int64_t star_stride, const int32_t* star_pa, int64_t n_stars,
+                            int32_t n_segments, int32_t pa_limit, float* av_out,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * No counterpart in rubix (rubix has no C interface; JAX allocates its buffers).
  *
  * rubix_cube_fwd without the workspace argument, for callers that cannot allocate

@@ -391,10 +391,15 @@ def particle_spectra(mass, metallicity, age, v_los, ssp_metallicity, ssp_age, ss
 def render_cube(coords, velocity, mass, metallicity, age, edges, sbin,
                 ssp_metallicity, ssp_age, ssp_flux, ssp_wave, dist_z, wave_t,
                 psf_size=None, psf_sigma=None, lsf_sigma=None, wave_res=None,
-                apply_filter=True, velocity_direction="z", chunk=512, rotation=None):
+                apply_filter=True, velocity_direction="z", chunk=512, rotation=None,
+                transmission=None):
     """The calc_ifu chain (rubix/config/pipeline_config.yml:1-60) from rotate_galaxy
     (when ``rotation`` = (halfmass_radius, alpha, beta, gamma) is given) or
-    filter_particles through convolve_lsf, noise excluded.  Returns a dict of stages."""
+    filter_particles through convolve_lsf, noise excluded.  Returns a dict of stages.
+
+    ``transmission`` ((n, L) array or a function of the (rotated, unfiltered)
+    coordinates returning one) multiplies the resampled spectra before the per-spaxel
+    sum: calculate_extinction of calc_dusty_ifu (pipeline_config.yml:62-136)."""
     coords = np.asarray(coords, dtype=np.float32)
     velocity = np.asarray(velocity, dtype=np.float32)
     mass = np.asarray(mass, dtype=np.float32)
@@ -411,6 +416,8 @@ def render_cube(coords, velocity, mass, metallicity, age, edges, sbin,
         out["mask"] = mask
     idx = square_spaxel_assignment(coords, edges)
     out["pixel_assignment"] = idx
+    if callable(transmission):
+        transmission = transmission(coords)
     wave_z = cosmological_doppler_shift(dist_z, ssp_wave)
     v_los = velocity[:, VELOCITY_AXIS[velocity_direction]]
     nseg = int(sbin) ** 2
@@ -420,6 +427,8 @@ def render_cube(coords, velocity, mass, metallicity, age, edges, sbin,
         e = min(n, s + chunk)
         sp = particle_spectra(mass[s:e], metallicity[s:e], age[s:e], v_los[s:e],
                               ssp_metallicity, ssp_age, ssp_flux, wave_z, wave_t)
+        if transmission is not None:
+            sp = sp * np.asarray(transmission[s:e], dtype=np.float64)
         ii = idx[s:e].astype(np.int64)
         keep = (ii >= 0) & (ii < nseg)
         np.add.at(cube, ii[keep], sp[keep])

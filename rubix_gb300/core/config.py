@@ -1,9 +1,9 @@
 """Configuration: the constants and pipeline definitions rubix keeps in YAML.
 
 ``rubix_config`` holds the entries of rubix/config/rubix_config.yml this path uses
-(``SPEED_OF_LIGHT`` :8, ``ifu.doppler.velocity_direction`` :241-245); ``PIPELINES`` holds
-the ``calc_ifu`` chain of rubix/config/pipeline_config.yml:1-60 as a dict (PyYAML is
-not a dependency).
+(constants :6-18, ``ssp.dust`` :145-150, ``ifu.doppler.velocity_direction`` :241-245);
+``PIPELINES`` holds the ``calc_ifu`` and ``calc_dusty_ifu`` chains of
+rubix/config/pipeline_config.yml:1-136 as dicts (PyYAML is not a dependency).
 """
 
 from __future__ import annotations
@@ -13,8 +13,13 @@ import json
 import os
 
 rubix_config = {
-    "constants": {"SPEED_OF_LIGHT": 299792.458},
+    "constants": {"SPEED_OF_LIGHT": 299792.458, "KPC_TO_CM": 3.08568e21,
+                  "MSUN_TO_GRAMS": 1.989e33, "MASS_OF_PROTON": 1.67262e-24},
     "ifu": {"doppler": {"velocity_direction": "z"}},
+    # rubix_config.yml:145-150; the dust step reads dust_to_gas_model and Xco from here
+    "ssp": {"dust": {"extinction_model": "Cardelli89", "Rv": 3.1,
+                     "dust_to_gas_model": "broken power law fit", "Xco": "Z",
+                     "dust_grain_density": 3.5}},
 }
 
 _CALC_IFU_ORDER = [
@@ -33,7 +38,13 @@ def _chain(names):
     return {"Transformers": out}
 
 
-PIPELINES = {"calc_ifu": _chain(_CALC_IFU_ORDER)}
+# rubix/config/pipeline_config.yml:62-136: calc_ifu with calculate_extinction between
+# the resampling and the datacube
+_CALC_DUSTY_IFU_ORDER = (_CALC_IFU_ORDER[:7] + ["calculate_extinction"]
+                         + _CALC_IFU_ORDER[7:])
+
+PIPELINES = {"calc_ifu": _chain(_CALC_IFU_ORDER),
+             "calc_dusty_ifu": _chain(_CALC_DUSTY_IFU_ORDER)}
 
 
 def get_config(config):

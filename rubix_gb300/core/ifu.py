@@ -38,6 +38,9 @@ class ParticleSpectra:
     stage "lookup":    SSP lookup at (metallicity, age)        -> [1, N, n_lambda_ssp]
     stage "mass":      times mass                              -> [1, N, n_lambda_ssp]
     stage "resampled": Doppler shifted and resampled to wave_t -> [1, N, n_lambda_t]
+
+    ``dust_av`` / ``dust_exponent`` (set by ``calculate_extinction``): every resampled
+    spectrum is multiplied by its dust transmission 2^(dust_exponent[t] * dust_av[i]).
     """
 
     stage: str
@@ -51,6 +54,8 @@ class ParticleSpectra:
     wave_z: Optional[torch.Tensor] = None
     wave_t: Optional[torch.Tensor] = None
     device_axis: bool = True
+    dust_av: Optional[torch.Tensor] = None
+    dust_exponent: Optional[torch.Tensor] = None
 
     @property
     def n(self) -> int:
@@ -78,7 +83,8 @@ class ParticleSpectra:
             offs = torch.arange(n + 1, dtype=torch.int32, device=self.device)
             out = ops.cube_forward(flux, zg, ag, self.wave_z, self.wave_t, self.mass,
                                    self.metallicity, self.age, self.velocity, self.velocity_axis,
-                                   ident, offs, n)
+                                   ident, offs, n, dust_av=self.dust_av,
+                                   dust_exponent=self.dust_exponent)
         return out.reshape(self.shape)
 
     def __array__(self, dtype=None, copy=None):
@@ -208,7 +214,8 @@ def get_calculate_datacube(config: dict) -> Callable:
             flux, zg, ag, _ = spec.ssp.device_arrays(dev)
             cube = ops.cube_forward(flux, zg, ag, spec.wave_z, spec.wave_t, spec.mass,
                                     spec.metallicity, spec.age, spec.velocity,
-                                    spec.velocity_axis, perm, offs, nseg)
+                                    spec.velocity_axis, perm, offs, nseg, dust_av=spec.dust_av,
+                                    dust_exponent=spec.dust_exponent)
         else:
             rows = _spectra_tensor(spec, dev)
             cube = ops.segment_sum_rows(rows, perm, offs, nseg)

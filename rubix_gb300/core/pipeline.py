@@ -16,6 +16,7 @@ from ..logging import get_logger
 from ..pipeline import LinearTransformerPipeline
 from .config import get_config, get_pipeline_config
 from .data import RubixData, get_reshape_data
+from .dust import get_extinction
 from .ifu import (get_calculate_datacube, get_calculate_spectra,
                   get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
 from .lsf import get_convolve_lsf
@@ -40,12 +41,17 @@ class RubixPipeline:
 
     def _get_pipeline_functions(self) -> list:
         c = self.user_config
-        return [
+        funcs = [
             get_galaxy_rotation(c), get_filter_particles(c), get_spaxel_assignment(c),
             get_calculate_spectra(c), get_reshape_data(c), get_scale_spectrum_by_mass(c),
             get_doppler_shift_and_resampling(c), get_calculate_datacube(c),
             get_convolve_psf(c), get_convolve_lsf(c), get_apply_noise(c),
         ]
+        # rubix builds calculate_extinction for every pipeline (core/pipeline.py:114);
+        # here it is built when the configuration has a dust section
+        if "dust" in c.get("ssp", {}):
+            funcs.insert(7, get_extinction(c))
+        return funcs
 
     def run(self) -> RubixData:
         t0 = time.time()

@@ -60,6 +60,7 @@ struct MainArgs {
   int chunk;            // particles per work item
   int lsf_k, lsf_crop;  // lsf_k = 0: no LSF epilogue
   float lsf[kMaxLsfTaps + 1];
+  const float* dust_e2;  // per telescope wavelength: -0.4 log2(10) A(lambda)/A(V)
 };
 
 // Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned): the TMA
@@ -525,7 +526,7 @@ __device__ __forceinline__ void lsf_epilogue_k(const MainArgs& a,
   }
 }
 
-template <int R>
+template <int R, bool kDust>
 __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout SL = smem_layout(a.n_wave, a.row_cap);
@@ -667,9 +668,25 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       const float beta0 = __shfl_sync(0xffffffffu, beta_l, 0);
       const float beta1 = __shfl_sync(0xffffffffu, beta_l, 8);
       const float beta2 = __shfl_sync(0xffffffffu, beta_l, 16);
+      if constexpr (kDust) {
+        // transmission 10^(-0.4 A(lambda)/A(V) A_V) of each particle's dust column
+        // (spectra/dust/dust_baseclasses.py:163-164) applied to its resampled spectrum
+        const float av0 = recs[0].c.w;
+        const float av1 = cnt > 1 ? recs[1].c.w : 0.f;
+        const float av2 = cnt > 2 ? recs[2].c.w : 0.f;
 #pragma unroll
-      for (int r = 0; r < R; ++r)
-        acc[r] = fmaf(beta2, I[2][r], fmaf(beta1, I[1][r], fmaf(beta0, I[0][r], acc[r])));
+        for (int r = 0; r < R; ++r) {
+          const float e2 = __ldg(a.dust_e2 + min(t0 + r, n_t - 1));
+          const float g0 = __fmul_rn(beta0, exp2f(__fmul_rn(e2, av0)));
+          const float g1 = __fmul_rn(beta1, exp2f(__fmul_rn(e2, av1)));
+          const float g2 = __fmul_rn(beta2, exp2f(__fmul_rn(e2, av2)));
+          acc[r] = fmaf(g2, I[2][r], fmaf(g1, I[1][r], fmaf(g0, I[0][r], acc[r])));
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          acc[r] = fmaf(beta2, I[2][r], fmaf(beta1, I[1][r], fmaf(beta0, I[0][r], acc[r])));
+      }
       p0 = p1;
       bp = bn;
     }
@@ -731,25 +748,42 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   }
 }
 
-template <int R>
-int launch_main(const MainArgs& args, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(cube_main_kernel<R>,
+template <int R, bool kDust>
+int launch_main_t(const MainArgs& args, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(cube_main_kernel<R, kDust>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess)
     return set_error(RUBIX_E_CUDA, "cudaFuncSetAttribute(cube_main_kernel): %s",
                      cudaGetErrorString(e));
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_main_kernel<R>, kAccThreads,
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_main_kernel<R, kDust>,
+                                                    kAccThreads,
                                                     smem);
   if (e != cudaSuccess || per_sm < 1)
     return set_error(RUBIX_E_UNSUPPORTED,
                      "cube_main_kernel does not fit on an SM with %zu bytes of shared memory",
                      smem);
   const int grid = sm_count() * per_sm;
-  cube_main_kernel<R><<<grid, kAccThreads, smem, st>>>(args);
+  cube_main_kernel<R, kDust><<<grid, kAccThreads, smem, st>>>(args);
   RUBIX_LAUNCH_CHECK("cube_main_kernel");
   return RUBIX_OK;
 }
+
+template <int R>
+int launch_main(const MainArgs& args, size_t smem, cudaStream_t st) {
+  return args.dust_e2 ? launch_main_t<R, true>(args, smem, st)
+                      : launch_main_t<R, false>(args, smem, st);
+}
+
+int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metallicity,
+                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met, int32_t n_age,
+                  int32_t n_wave, const float* wave_t, int32_t n_wave_t, const float* mass,
+                  const float* metallicity, const float* age, const float* velocity,
+                  int64_t vel_stride, int32_t vel_component, const int32_t* perm,
+                  const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                  const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop, const float* av,
+                  const float* dust_e2, float* cube, int64_t spaxel_stride, void* workspace,
+                  size_t workspace_bytes, void* stream);
 
 }  // namespace
 }  // namespace rubix
@@ -764,50 +798,51 @@ extern "C" size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32
       .bytes;
 }
 
-extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,
-                              const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
-                              int32_t n_age, int32_t n_wave, const float* wave_t,
-                              int32_t n_wave_t, const float* mass, const float* metallicity,
-                              const float* age, const float* velocity, int64_t vel_stride,
-                              int32_t vel_component, const int32_t* perm,
-                              const int32_t* seg_offsets, int32_t n_segments, int64_t n,
-                              const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
-                              float* cube, int64_t spaxel_stride, void* workspace,
-                              size_t workspace_bytes, void* stream) {
-  RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "rubix_cube_fwd: bad n");
-  RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "rubix_cube_fwd: n_segments < 0");
+namespace rubix {
+namespace {
+
+int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metallicity,
+                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met, int32_t n_age,
+                  int32_t n_wave, const float* wave_t, int32_t n_wave_t, const float* mass,
+                  const float* metallicity, const float* age, const float* velocity,
+                  int64_t vel_stride, int32_t vel_component, const int32_t* perm,
+                  const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                  const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop, const float* av,
+                  const float* dust_e2, float* cube, int64_t spaxel_stride, void* workspace,
+                  size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "%s: bad n", who);
+  RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "%s: n_segments < 0", who);
   RUBIX_REQUIRE(n_met >= 2 && n_age >= 2, RUBIX_E_SHAPE,
-                "rubix_cube_fwd: SSP grid needs >= 2 metallicities and >= 2 ages");
-  RUBIX_REQUIRE(n_wave >= 2, RUBIX_E_SHAPE, "rubix_cube_fwd: SSP grid needs >= 2 wavelengths");
+                "%s: SSP grid needs >= 2 metallicities and >= 2 ages", who);
+  RUBIX_REQUIRE(n_wave >= 2, RUBIX_E_SHAPE, "%s: SSP grid needs >= 2 wavelengths", who);
   RUBIX_REQUIRE(n_wave_t >= 1 && n_wave_t <= kMaxWaveT, RUBIX_E_SHAPE,
-                "rubix_cube_fwd: n_wave_t must be in [1, %d], got %d", kMaxWaveT, n_wave_t);
+                "%s: n_wave_t must be in [1, %d], got %d", who, kMaxWaveT, n_wave_t);
   RUBIX_REQUIRE(spaxel_stride >= n_wave_t, RUBIX_E_SHAPE,
-                "rubix_cube_fwd: spaxel_stride < n_wave_t");
+                "%s: spaxel_stride < n_wave_t", who);
   RUBIX_REQUIRE(vel_component >= 0 && vel_component < vel_stride, RUBIX_E_INVALID,
-                "rubix_cube_fwd: vel_component outside the velocity row");
+                "%s: vel_component outside the velocity row", who);
   RUBIX_REQUIRE(n_lsf_taps >= 0 && n_lsf_taps <= kMaxLsfTaps, RUBIX_E_SHAPE,
-                "rubix_cube_fwd: at most %d LSF taps", kMaxLsfTaps);
+                "%s: at most %d LSF taps", who, kMaxLsfTaps);
   RUBIX_REQUIRE(n_lsf_taps == 0 || (lsf_taps && lsf_crop >= 0 && lsf_crop < n_lsf_taps),
-                RUBIX_E_INVALID, "rubix_cube_fwd: bad LSF taps/crop");
+                RUBIX_E_INVALID, "%s: bad LSF taps/crop", who);
   if (n_segments == 0) return RUBIX_OK;
   RUBIX_REQUIRE(ssp_flux && ssp_metallicity && ssp_age && ssp_wave_z && wave_t && seg_offsets &&
                     cube,
-                RUBIX_E_INVALID, "rubix_cube_fwd: null pointer");
+                RUBIX_E_INVALID, "%s: null pointer", who);
   RUBIX_REQUIRE(n == 0 || (mass && metallicity && age && velocity && perm), RUBIX_E_INVALID,
-                "rubix_cube_fwd: null particle pointer");
+                "%s: null particle pointer", who);
   const size_t need = rubix_cube_workspace_size(n, n_segments, n_wave_t, n_met, n_age, n_wave);
   RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
-                "rubix_cube_fwd: workspace of %zu bytes needed, %zu given", need,
-                workspace_bytes);
+                "%s: workspace of %zu bytes needed, %zu given", who, need, workspace_bytes);
   RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
-                "rubix_cube_fwd: workspace must be 256-byte aligned");
+                "%s: workspace must be 256-byte aligned", who);
   const int row_cap = n_wave + 2;
   const SmemLayout SL = smem_layout(n_wave, row_cap);
   // Up to about 1300 SSP wavelengths two blocks fit on an SM; larger grids run one.
   RUBIX_REQUIRE(SL.total <= 227 * 1024, RUBIX_E_UNSUPPORTED,
-                "rubix_cube_fwd: SSP grid of %d wavelengths needs %zu bytes of shared memory "
+                "%s: SSP grid of %d wavelengths needs %zu bytes of shared memory "
                 "(limit 232448)",
-                n_wave, SL.total);
+                who, n_wave, SL.total);
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const CubeTuning tune = cube_tuning_current();
@@ -815,7 +850,7 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
       carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave, tune.chunk);
   const CubeInputs in{ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met, n_age, n_wave,
                       wave_t, n_wave_t, mass, metallicity, age, velocity, vel_stride,
-                      vel_component, perm, seg_offsets, n_segments, n};
+                      vel_component, perm, seg_offsets, n_segments, n, av};
   {
     const int rc = cube_prepare(in, L, tune, /*with_grad=*/false, st);
     if (rc != RUBIX_OK) return rc;
@@ -844,6 +879,7 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
   args.lsf_k = n_lsf_taps;
   args.lsf_crop = lsf_crop;
   for (int i = 0; i <= kMaxLsfTaps; ++i) args.lsf[i] = i < n_lsf_taps ? lsf_taps[i] : 0.f;
+  args.dust_e2 = dust_e2;
   const int need_r = (n_wave_t + kAccThreads - 1) / kAccThreads;
   const size_t smem = SL.total;
   if (need_r <= 1) return launch_main<1>(args, smem, st);
@@ -853,6 +889,46 @@ extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicit
   if (need_r <= 8) return launch_main<8>(args, smem, st);
   if (need_r <= 10) return launch_main<10>(args, smem, st);
   return launch_main<11>(args, smem, st);  // kAccThreads * 11 >= kMaxWaveT
+}
+
+}  // namespace
+}  // namespace rubix
+
+extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,
+                              const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                              int32_t n_age, int32_t n_wave, const float* wave_t,
+                              int32_t n_wave_t, const float* mass, const float* metallicity,
+                              const float* age, const float* velocity, int64_t vel_stride,
+                              int32_t vel_component, const int32_t* perm,
+                              const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                              const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
+                              float* cube, int64_t spaxel_stride, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+  return cube_fwd_impl("rubix_cube_fwd", ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met,
+                       n_age, n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity,
+                       vel_stride, vel_component, perm, seg_offsets, n_segments, n, lsf_taps,
+                       n_lsf_taps, lsf_crop, nullptr, nullptr, cube, spaxel_stride, workspace,
+                       workspace_bytes, stream);
+}
+
+extern "C" int rubix_cube_fwd_dust(const float* ssp_flux, const float* ssp_metallicity,
+                                   const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                                   int32_t n_age, int32_t n_wave, const float* wave_t,
+                                   int32_t n_wave_t, const float* mass, const float* metallicity,
+                                   const float* age, const float* velocity, int64_t vel_stride,
+                                   int32_t vel_component, const float* av,
+                                   const float* ext_exponent, const int32_t* perm,
+                                   const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                   const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
+                                   float* cube, int64_t spaxel_stride, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(ext_exponent != nullptr && (n == 0 || av != nullptr), RUBIX_E_INVALID,
+                "rubix_cube_fwd_dust: null A_V or extinction exponent");
+  return cube_fwd_impl("rubix_cube_fwd_dust", ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z,
+                       n_met, n_age, n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity,
+                       vel_stride, vel_component, perm, seg_offsets, n_segments, n, lsf_taps,
+                       n_lsf_taps, lsf_crop, av, ext_exponent, cube, spaxel_stride, workspace,
+                       workspace_bytes, stream);
 }
 
 extern "C" int rubix_cube_status(const void* workspace, int* device_error, void* stream) {

@@ -45,7 +45,7 @@ struct ParticleRec {  // 48 bytes, three vector loads
   float4 a;  // mass, alpha, B = (v/c)/h in bucket units, tz
   int4 b;    // cell (iz*(nA-1)+ia, -1 outside the grid), kstart, kend|flags, ta bits
   float4 c;  // T = in-range flux sum of the mixed template, dT/dZ, dT/dage (gradient
-             // passes only), unused
+             // passes only), A_V of the dust in front of the particle (0 without dust)
 };
 
 __device__ __forceinline__ int count_le_scaled(const float* __restrict__ wz, int n, float alpha,
@@ -183,7 +183,8 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
                                    const float* __restrict__ wave_t, int n_t,
                                    const double* __restrict__ prefix,
                                    const CubeCtrl* __restrict__ ctrl,
-                                   ParticleRec* __restrict__ rec, int with_grad) {
+                                   ParticleRec* __restrict__ rec, int with_grad,
+                                   const float* __restrict__ av) {
   const long long n_valid = seg_off[n_seg];
   const float t_lo = wave_t[0], t_hi = wave_t[n_t - 1];
   const double h = ctrl->h;
@@ -247,7 +248,7 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
     ParticleRec r;
     r.a = make_float4(m, alpha, B, tz);
     r.b = make_int4(cell, ks, ke | (coarse ? 0 : kGenericFlag), __float_as_int(ta));
-    r.c = make_float4((float)T, (float)TZ, (float)TA, 0.f);
+    r.c = make_float4((float)T, (float)TZ, (float)TA, av ? av[i] : 0.f);
     rec[j] = r;
   }
 }
@@ -351,6 +352,7 @@ struct CubeInputs {
   const int* seg_off;
   int n_seg;
   long long n;
+  const float* av = nullptr;  // per-particle A_V (dust), input order; nullptr: none
 };
 
 // Launches the setup passes into the carved workspace: bucket table, corner table,
@@ -383,7 +385,7 @@ inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, const CubeTun
                                           in.vel_comp, in.perm, in.seg_off, in.n_seg, in.n,
                                           in.ssp_met, in.n_met, in.ssp_age, in.n_age,
                                           in.ssp_wave_z, in.n_wave, in.wave_t, in.n_wave_t,
-                                          L.prefix, L.ctrl, L.rec, with_grad ? 1 : 0);
+                                          L.prefix, L.ctrl, L.rec, with_grad ? 1 : 0, in.av);
     RUBIX_LAUNCH_CHECK("cube_gather_kernel");
   }
   {

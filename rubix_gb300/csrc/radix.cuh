@@ -1,0 +1,131 @@
+// Stable LSD radix sort of (32-bit key, int value) pairs, 8 bits per pass, written
+// from the published LSD scheme: per pass, a per-tile digit histogram, one exclusive
+// scan over (digit, tile), and a stable scatter in which each tile ranks its keys with
+// warp-level match/popc and per-warp digit counters.  Deterministic.
+#pragma once
+
+#include "common.cuh"
+#include "scan.cuh"
+
+namespace rubix {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+
+// Per-tile histogram of one digit; hist is digit-major: hist[d * n_tiles + tile].
+__global__ void __launch_bounds__(kSortThreads)
+radix_hist_kernel(const unsigned* __restrict__ keys, long long n, int shift,
+                  unsigned digit_mask, int n_tiles, int* __restrict__ hist) {
+  __shared__ int s_hist[kRadix];
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) s_hist[d] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kSortTile;
+  for (int it = 0; it < kSortItems; ++it) {
+    long long e = base + it * kSortThreads + threadIdx.x;
+    if (e < n) atomicAdd(&s_hist[(keys[e] >> shift) & digit_mask], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d <= (int)digit_mask; d += blockDim.x)
+    hist[(long long)d * n_tiles + blockIdx.x] = s_hist[d];
+}
+
+// Stable scatter of one digit pass.  Warp w of the tile owns the contiguous keys
+// [base + w*512, base + (w+1)*512) and walks them in 16 rounds of 32, so
+// (warp, round, lane) order equals input order.
+__global__ void __launch_bounds__(kSortThreads)
+radix_scatter_kernel(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
+                     unsigned* __restrict__ keys_out, int* __restrict__ vals_out, long long n,
+                     int shift, unsigned digit_mask, int n_tiles,
+                     const int* __restrict__ hist_scanned) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ int s_cnt[kWarps][kRadix];
+  __shared__ int s_base[kRadix];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
+  const int n_digits = (int)digit_mask + 1;
+  for (int d = threadIdx.x; d < n_digits; d += kSortThreads)
+    s_base[d] = hist_scanned[(long long)d * n_tiles + blockIdx.x];
+  __syncthreads();
+
+  const long long wbase = (long long)blockIdx.x * kSortTile + (long long)warp * (32 * kSortItems);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned key[kSortItems];
+  int val[kSortItems];
+  int rank[kSortItems];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    long long e = wbase + r * 32 + lane;
+    bool valid = e < n;
+    key[r] = valid ? keys_in[e] : 0u;
+    val[r] = valid ? vals_in[e] : 0;
+    int d = valid ? (int)((key[r] >> shift) & digit_mask) : kRadix;  // kRadix: own group
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int before = valid ? s_cnt[warp][d] : 0;
+    rank[r] = before + __popc(peers & lt_mask);
+    __syncwarp();
+    if (valid && (peers & lt_mask) == 0) s_cnt[warp][d] = before + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // Exclusive prefix over warps, per digit.
+  for (int d = threadIdx.x; d < n_digits; d += kSortThreads) {
+    int run = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      int c = s_cnt[w][d];
+      s_cnt[w][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    long long e = wbase + r * 32 + lane;
+    if (e < n) {
+      int d = (int)((key[r] >> shift) & digit_mask);
+      long long pos = (long long)s_base[d] + s_cnt[warp][d] + rank[r];
+      keys_out[pos] = key[r];
+      vals_out[pos] = val[r];
+    }
+  }
+}
+
+inline long long radix_tiles(long long n) {
+  const long long t = (n + kSortTile - 1) / kSortTile;
+  return t < 1 ? 1 : t;
+}
+
+// Sorts n pairs by bits [0, bits) of the keys, stably, ping-ponging between (k0, v0)
+// and (k1, v1); `hist` holds kRadix * radix_tiles(n) ints.  Returns 0 when the sorted
+// pairs end in (k0, v0), 1 when in (k1, v1).  bits = 0 sorts nothing.
+inline int radix_sort_pairs(unsigned* k0, int* v0, unsigned* k1, int* v1, long long n, int bits,
+                            int* hist, cudaStream_t st) {
+  const int n_tiles = (int)radix_tiles(n);
+  unsigned* kin = k0;
+  unsigned* kout = k1;
+  int* vin = v0;
+  int* vout = v1;
+  int where = 0;
+  for (int shift = 0; shift < bits; shift += kRadixBits) {
+    const unsigned dmask = (unsigned)(kRadix - 1);
+    radix_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, n, shift, dmask, n_tiles, hist);
+    scan_exclusive_1block<<<1, 1024, 0, st>>>(hist, (long long)kRadix * n_tiles, 0);
+    radix_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, vin, kout, vout, n, shift, dmask,
+                                                           n_tiles, hist);
+    unsigned* tk = kin;
+    kin = kout;
+    kout = tk;
+    int* tv = vin;
+    vin = vout;
+    vout = tv;
+    where ^= 1;
+  }
+  return where;
+}
+
+}  // namespace
+}  // namespace rubix

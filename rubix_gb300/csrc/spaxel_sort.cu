@@ -6,16 +6,12 @@
 // which each tile ranks its keys with warp-level match/popc and per-warp digit
 // counters.  No float atomics anywhere; the result is deterministic.
 #include "common.cuh"
+#include "radix.cuh"
 #include "scan.cuh"
 
 namespace rubix {
 namespace {
 
-constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
-constexpr int kRadixBits = 8;
-constexpr int kRadix = 1 << kRadixBits;
 constexpr int kMaxSmemEdges = 8192;
 
 // Number of edges <= x (searchsorted side='right'); NaN counts as above all edges,
@@ -84,84 +80,6 @@ __global__ void make_keys_kernel(const int* __restrict__ idx,
     bool ok = (k >= 0) && (k < n_segments) && (keep == nullptr || keep[i] != 0);
     keys[i] = ok ? (unsigned)k : (unsigned)n_segments;
     vals[i] = (int)i;
-  }
-}
-
-// Per-tile histogram of one digit; hist is digit-major: hist[d * n_tiles + tile].
-__global__ void __launch_bounds__(kSortThreads)
-radix_hist_kernel(const unsigned* __restrict__ keys, long long n, int shift,
-                  unsigned digit_mask, int n_tiles, int* __restrict__ hist) {
-  __shared__ int s_hist[kRadix];
-  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) s_hist[d] = 0;
-  __syncthreads();
-  const long long base = (long long)blockIdx.x * kSortTile;
-  for (int it = 0; it < kSortItems; ++it) {
-    long long e = base + it * kSortThreads + threadIdx.x;
-    if (e < n) atomicAdd(&s_hist[(keys[e] >> shift) & digit_mask], 1);
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d <= (int)digit_mask; d += blockDim.x)
-    hist[(long long)d * n_tiles + blockIdx.x] = s_hist[d];
-}
-
-// Stable scatter of one digit pass.  Warp w of the tile owns the contiguous keys
-// [base + w*512, base + (w+1)*512) and walks them in 16 rounds of 32, so
-// (warp, round, lane) order equals input order.
-__global__ void __launch_bounds__(kSortThreads)
-radix_scatter_kernel(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
-                     unsigned* __restrict__ keys_out, int* __restrict__ vals_out, long long n,
-                     int shift, unsigned digit_mask, int n_tiles,
-                     const int* __restrict__ hist_scanned) {
-  constexpr int kWarps = kSortThreads / 32;
-  __shared__ int s_cnt[kWarps][kRadix];
-  __shared__ int s_base[kRadix];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
-  const int n_digits = (int)digit_mask + 1;
-  for (int d = threadIdx.x; d < n_digits; d += kSortThreads)
-    s_base[d] = hist_scanned[(long long)d * n_tiles + blockIdx.x];
-  __syncthreads();
-
-  const long long wbase = (long long)blockIdx.x * kSortTile + (long long)warp * (32 * kSortItems);
-  const unsigned lt_mask = (1u << lane) - 1u;
-  unsigned key[kSortItems];
-  int val[kSortItems];
-  int rank[kSortItems];
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    long long e = wbase + r * 32 + lane;
-    bool valid = e < n;
-    key[r] = valid ? keys_in[e] : 0u;
-    val[r] = valid ? vals_in[e] : 0;
-    int d = valid ? (int)((key[r] >> shift) & digit_mask) : kRadix;  // kRadix: own group
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    int before = valid ? s_cnt[warp][d] : 0;
-    rank[r] = before + __popc(peers & lt_mask);
-    __syncwarp();
-    if (valid && (peers & lt_mask) == 0) s_cnt[warp][d] = before + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  // Exclusive prefix over warps, per digit.
-  for (int d = threadIdx.x; d < n_digits; d += kSortThreads) {
-    int run = 0;
-#pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      int c = s_cnt[w][d];
-      s_cnt[w][d] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    long long e = wbase + r * 32 + lane;
-    if (e < n) {
-      int d = (int)((key[r] >> shift) & digit_mask);
-      long long pos = (long long)s_base[d] + s_cnt[warp][d] + rank[r];
-      keys_out[pos] = key[r];
-      vals_out[pos] = val[r];
-    }
   }
 }
 

@@ -26,6 +26,9 @@ __all__ = [
     "flux_image",
     "noise_median",
     "apply_noise_",
+    "dust_gas_extinction",
+    "dust_av",
+    "dust_apply_rows_",
     "workspace",
 ]
 
@@ -120,12 +123,14 @@ def spaxel_sort(idx: torch.Tensor, n_segments: int, keep: torch.Tensor | None = 
 
 def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, metallicity,
                  age, velocity, vel_component, perm, seg_offsets, n_segments, out=None,
-                 lsf_taps=None, lsf_crop=0, check=False):
+                 lsf_taps=None, lsf_crop=0, check=False, dust_av=None, dust_exponent=None):
     """Fused lookup + mass + Doppler/resample + per-spaxel sum -> cube [n_segments, L].
 
     ``lsf_taps`` (optional) adds the LSF convolution along wavelength of every finished
-    spectrum.  ``check=True`` synchronises the stream and raises if the kernel reported
-    a device error (a timed-out shared-memory copy wait)."""
+    spectrum.  ``dust_av`` ([n], A_V per particle) with ``dust_exponent`` ([L],
+    -0.4 log2(10) A(lambda)/A(V)) multiplies every resampled spectrum by its dust
+    transmission before the sum.  ``check=True`` synchronises the stream and raises if
+    the kernel reported a device error (a timed-out shared-memory copy wait)."""
     ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
     if ssp_flux.dim() != 3:
         raise ValueError("ssp_flux must be [n_met, n_age, n_wave]")
@@ -157,12 +162,27 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
     lsf = None if lsf_taps is None else _host_taps(lsf_taps)
     nbytes = _lib.query("rubix_cube_workspace_size", n, int(n_segments), L, nz, na, nw)
     ws = workspace(nbytes, dev)
-    _lib.call("rubix_cube_fwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
-              _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
-              _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
-              _ptr(seg_offsets), int(n_segments), n,
-              None if lsf is None else lsf.ctypes.data, 0 if lsf is None else lsf.size,
-              int(lsf_crop), _ptr(out), out.stride(0), _ptr(ws), ws.numel(), _stream(dev))
+    lsf_args = (None if lsf is None else lsf.ctypes.data, 0 if lsf is None else lsf.size,
+                int(lsf_crop))
+    if (dust_av is None) != (dust_exponent is None):
+        raise ValueError("dust_av and dust_exponent go together")
+    if dust_av is None:
+        _lib.call("rubix_cube_fwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
+                  _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
+                  _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
+                  _ptr(seg_offsets), int(n_segments), n, *lsf_args, _ptr(out), out.stride(0),
+                  _ptr(ws), ws.numel(), _stream(dev))
+    else:
+        dust_av = _contig("dust_av", dust_av, torch.float32).reshape(-1)
+        dust_exponent = _contig("dust_exponent", dust_exponent, torch.float32).reshape(-1)
+        if dust_av.numel() != n or dust_exponent.numel() != L:
+            raise ValueError("dust_av must be [n] and dust_exponent [L]")
+        _lib.call("rubix_cube_fwd_dust", _ptr(ssp_flux), _ptr(ssp_metallicity),
+                  _ptr(ssp_age), _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass),
+                  _ptr(metallicity), _ptr(age), _ptr(velocity), vstride, int(vel_component),
+                  _ptr(dust_av), _ptr(dust_exponent), _ptr(perm), _ptr(seg_offsets),
+                  int(n_segments), n, *lsf_args, _ptr(out), out.stride(0), _ptr(ws),
+                  ws.numel(), _stream(dev))
     # setup, corner table, prefix, count, scans (one launch), fill, main (+ gather)
     _count((7 + (1 if n > 0 else 0)) if n_segments > 0 else 0)
     if check and n_segments > 0:
@@ -430,3 +450,70 @@ def mask_zero_(values, mask):
     _lib.call("rubix_mask_zero", _ptr(values), n, width, width, _ptr(mask), _stream(values.device))
     _count(1 if values.numel() > 0 else 0)
     return values
+
+
+def dust_gas_extinction(mass, metals, dgr_params, broken: bool, scale: float,
+                        spaxel_area: float, h_col: int = 0, o_col: int = 4) -> torch.Tensor:
+    """Per-cell extinction of the gas [n] float32: mass * dust-to-gas ratio of
+    12 + log10(O/(16 H)) * scale / spaxel_area (``rubix_dust_gas_extinction``)."""
+    mass = _contig("mass", mass, torch.float32).reshape(-1)
+    metals = _contig("metals", metals, torch.float32)
+    n = mass.numel()
+    rows = metals.reshape(n, -1) if n > 0 else metals.reshape(0, max(h_col, o_col) + 1)
+    prm = np.ascontiguousarray(np.asarray(dgr_params, dtype=np.float32).reshape(6))
+    out = torch.empty(n, dtype=torch.float32, device=mass.device)
+    _lib.call("rubix_dust_gas_extinction", _ptr(mass), _ptr(rows), rows.shape[1], int(h_col),
+              int(o_col), n, prm.ctypes.data, 1 if broken else 0, float(scale),
+              float(spaxel_area), _ptr(out), _stream(mass.device))
+    _count(1 if n > 0 else 0)
+    return out
+
+
+def dust_av(gas_coords, gas_pa, gas_ext, star_coords, star_pa, n_segments: int,
+            pa_limit: int) -> torch.Tensor:
+    """A_V [n_stars] float32 of every star (``rubix_dust_av``): rubix's interpolated
+    cumulative dust column of the star's spaxel at the star's z."""
+    star_coords = _contig("star_coords", star_coords, torch.float32).reshape(-1, 3)
+    star_pa = _contig("star_pa", star_pa, torch.int32).reshape(-1)
+    gas_coords = _contig("gas_coords", gas_coords, torch.float32).reshape(-1, 3)
+    gas_pa = _contig("gas_pa", gas_pa, torch.int32).reshape(-1)
+    gas_ext = _contig("gas_ext", gas_ext, torch.float32).reshape(-1)
+    ns, ng = star_coords.shape[0], gas_coords.shape[0]
+    if star_pa.numel() != ns or gas_pa.numel() != ng or gas_ext.numel() != ng:
+        raise ValueError("per-star / per-cell arrays must match the coordinates")
+    dev = star_coords.device
+    out = torch.empty(ns, dtype=torch.float32, device=dev)
+    ws = workspace(_lib.query("rubix_dust_av_workspace_size", ng, int(n_segments)), dev)
+    _lib.call("rubix_dust_av", _ptr(gas_coords), 3, _ptr(gas_pa), _ptr(gas_ext), ng,
+              _ptr(star_coords), 3, _ptr(star_pa), ns, int(n_segments), int(pa_limit),
+              _ptr(out), _ptr(ws), ws.numel(), _stream(dev))
+    if ns > 0:
+        k = 1  # star pass
+        if ng > 0:
+            # z sort, assignment sort, G sort (4 + P + 4 radix passes of 3 launches each)
+            # plus the key, offset, cumulative-sum, node, run and scan passes
+            k += 35 + 3 * _key_passes(int(pa_limit) - 1)
+            if pa_limit > n_segments:
+                k += 14 + 3 * _key_passes(int(n_segments) - 1)
+        _count(k)
+    return out
+
+
+def dust_apply_rows_(rows: torch.Tensor, av, exponent) -> torch.Tensor:
+    """In place: rows [n, L] *= 2^(exponent[t] * av[i]) (``rubix_dust_apply_rows``)."""
+    _check_cuda("rows", rows, torch.float32)
+    if rows.dim() != 2 or rows.stride(1) != 1:
+        raise ValueError("rows must be [n, L] with unit stride along wavelength")
+    av = _contig("av", av, torch.float32).reshape(-1)
+    exponent = _contig("exponent", exponent, torch.float32).reshape(-1)
+    n, L = rows.shape
+    if av.numel() != n or exponent.numel() != L:
+        raise ValueError("av must be [n] and exponent [L]")
+    _lib.call("rubix_dust_apply_rows", _ptr(rows), n, L, rows.stride(0), _ptr(av),
+              _ptr(exponent), _stream(rows.device))
+    _count(1 if n * L > 0 else 0)
+    return rows
+
+
+def _key_passes(max_key: int) -> int:
+    return (max(int(max_key), 0).bit_length() + 7) // 8

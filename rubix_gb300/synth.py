@@ -15,6 +15,8 @@ generated from a fixed ``numpy.random.Generator(PCG64(seed))``:
 * Edge cases appended on request: particles exactly on interior and outer spaxel
   edges, outside the field of view, ages/metallicities on grid nodes and outside
   the grid, zero mass.
+* Gas disk (for dust extinction): exponential in R and z, log-normal masses, metal
+  mass fractions with 12 + log(O/H) spread around solar.
 """
 
 from __future__ import annotations
@@ -101,6 +103,41 @@ def make_galaxy(n: int, seed: int = 0, R_d: float = 3.0, h_z: float = 0.3, v_rot
     return ParticleData(coords=pos[perm].astype(np.float32), velocity=vel[perm].astype(np.float32),
                         mass=mass[perm].astype(np.float32), metallicity=met[perm].astype(np.float32),
                         age=age[perm].astype(np.float32))
+
+
+@dataclass
+class GasData:
+    coords: np.ndarray  # [n, 3] kpc
+    mass: np.ndarray    # [n] Msun
+    metals: np.ndarray  # [n, 10] mass fractions: H, He, C, N, O, Ne, Mg, Si, Fe, total
+
+    @property
+    def n(self) -> int:
+        return int(self.mass.shape[0])
+
+
+def make_gas(n: int, seed: int = 0, R_d: float = 3.0, h_z: float = 0.15,
+             inclination_deg: float = 60.0, median_mass: float = 3e4) -> GasData:
+    """A gas disk for the dust step: exponential in R (scale R_d) and z (h_z), inclined
+    like the stellar disk; log-normal masses; hydrogen mass fraction 0.74 and oxygen
+    log-uniform in [1e-3, 2e-2] (12 + log(O/H) between about 7.9 and 9.2)."""
+    rng = np.random.Generator(np.random.PCG64(5000 + seed))
+    R = rng.gamma(2.0, R_d, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    zz = rng.laplace(0.0, h_z, n)
+    pos = np.stack([R * np.cos(phi), R * np.sin(phi), zz], axis=1)
+    inc = np.deg2rad(inclination_deg)
+    rot = np.array([[1, 0, 0], [0, np.cos(inc), -np.sin(inc)], [0, np.sin(inc), np.cos(inc)]])
+    pos = pos @ rot.T
+    mass = median_mass * np.exp(rng.normal(0.0, 0.5, n))
+    metals = np.zeros((n, 10))
+    metals[:, 0] = 0.74
+    metals[:, 1] = 0.25
+    metals[:, 4] = np.exp(rng.uniform(np.log(1e-3), np.log(2e-2), n))
+    metals[:, 2] = 0.2 * metals[:, 4]
+    metals[:, 9] = 1.0 - metals[:, 0] - metals[:, 1]
+    return GasData(coords=pos.astype(np.float32), mass=mass.astype(np.float32),
+                   metals=metals.astype(np.float32))
 
 
 def append_edge_cases(p: ParticleData, edges: np.ndarray, ssp: SSPData) -> ParticleData:
