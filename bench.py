@@ -322,6 +322,54 @@ def fwd_bwd_bench(dev, steps, warmup, flush):
                         "rendered from perturbed parameters"}
 
 
+def dusty_bench(dev, w, d_in, steps, warmup, flush, n_gas=500_000):
+    """The main step with calc_dusty_ifu's dust extinction: 5e5 gas cells -> per-cell
+    extinction -> A_V of every star (rubix's column interpolation) -> dusty accumulate
+    (+LSF), PSF, noise.  Also times the A_V passes and the dusty accumulate alone."""
+    import torch
+
+    from rubix_gb300 import ops, synth
+    from rubix_gb300.api import IFURenderer
+
+    g = synth.make_gas(n_gas, seed=2)
+    rnd = IFURenderer.from_workload(w, device=dev, dust={"extinction_model": "Cardelli89",
+                                                         "Rv": 3.1})
+    gas = tuple(torch.from_numpy(a).to(dev) for a in (g.coords, g.mass, g.metals))
+    N, L = w.particles.n, int(w.wave_t.size)
+    state = {}
+
+    def av_only():
+        idx, mask = rnd.assign(d_in[0])
+        state["sorted"] = rnd.sort(idx, mask)
+        state["av"] = rnd.dust_av(d_in[0], idx, *gas)
+
+    def step():
+        idx, mask = rnd.assign(d_in[0])
+        perm, offs = rnd.sort(idx, mask)
+        av = rnd.dust_av(d_in[0], idx, *gas)
+        cube = rnd.accumulate(d_in[2], d_in[3], d_in[4], d_in[1], perm, offs, with_lsf=True,
+                              dust_av=av)
+        return rnd.noise_(rnd.psf(cube))
+
+    n0 = ops.LAUNCHES["count"]
+    step()
+    launches = ops.LAUNCHES["count"] - n0
+    ms = _time_steps(step, steps, warmup, flush)
+    av_ms = _time_steps(av_only, steps, warmup, flush)
+    perm, offs = state["sorted"]
+    acc_ms = _time_steps(lambda: rnd.accumulate(d_in[2], d_in[3], d_in[4], d_in[1], perm, offs,
+                                                with_lsf=True, dust_av=state["av"]),
+                         steps, warmup, flush)
+    return {"metric": "particles*lambda/s, particle->IFU datacube forward with dust "
+                      "extinction (calc_dusty_ifu)",
+            "value": N * L / (ms * 1e-3), "unit": "particle*lambda/s", "ms_per_step": ms,
+            "assign_sort_av_ms": av_ms, "dusty_accumulate_ms": acc_ms,
+            "gpu_launches_per_step": launches,
+            "workload": f"ifu stars ({N}) + {n_gas} gas cells (exponential disk, h_z 0.15 "
+                        "kpc, log-normal masses, 12+log(O/H) 7.9-9.2), Cardelli89 R_V 3.1, "
+                        "broken power-law dust-to-gas ratio (X_CO = Z)"}
+
+
 # The plain GPU path: the same algorithm written with stock torch operations (gathers,
 # searchsorted, index_add_, conv2d, conv1d) on the same GPU, materialising the
 # per-particle spectra like the reference's step functions do.
@@ -632,6 +680,7 @@ def main():
                 ("plain_gpu", lambda: plain_bench(dev, w, rnd, d_in, ours_final, args.steps,
                                                   args.warmup, flush)),
                 ("plain_gpu_fwd_bwd", lambda: plain_fwd_bwd_bench(dev, args.steps, 1)),
+                ("dusty", lambda: dusty_bench(dev, w, d_in, args.steps, 3, flush)),
                 ("ragged", lambda: ragged_bench(dev, 3, 2))):
             try:
                 extras[name] = fn()

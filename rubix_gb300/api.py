@@ -5,7 +5,8 @@ redshifted SSP wavelengths, telescope wavelength grid, spatial bin edges, PSF an
 LSF taps) and runs the kernels of the C ABI for one set of particles:
 
     aperture mask -> spaxel assignment -> stable sort by spaxel
-    -> fused lookup/mass/Doppler/resample/accumulate -> PSF -> LSF
+    [-> A_V of every star from the gas (dust extinction, when configured)]
+    -> fused lookup/mass/Doppler/resample/(dust)/accumulate -> PSF -> LSF
 
 It is the engine behind the rubix-compatible step functions in ``rubix_gb300.core``
 (where each step stays separately callable) and the one-call path used for
@@ -20,6 +21,7 @@ from typing import Optional
 import numpy as np
 import torch
 
+from . import dust as dust_host
 from . import ops
 from . import telescope as tel
 
@@ -56,7 +58,8 @@ class IFURenderer:
                  sbin: int, dist_z: float, psf_taps=None, lsf_taps=None, lsf_crop: int = 12,
                  velocity_axis: int = 2, apply_filter: bool = True, device="cuda",
                  noise_s2n: Optional[float] = None, noise_distribution: str = "normal",
-                 noise_seed: int = 0):
+                 noise_seed: int = 0, dust: Optional[dict] = None,
+                 spaxel_area: Optional[float] = None):
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("IFURenderer needs a CUDA device (rubix_gb300 has no CPU path)")
@@ -80,14 +83,36 @@ class IFURenderer:
         self.noise_s2n = None if noise_s2n is None else float(noise_s2n)
         self.noise_distribution = noise_distribution
         self.noise_seed = int(noise_seed)
+        # dust: keys of rubix's ssp.dust config (extinction_model, Rv, dust_grain_density,
+        # dust_to_gas_model, Xco); spaxel_area in kpc^2 (square of the spatial bin size)
+        self.dust = None
+        if dust is not None:
+            d = dict(dust_host.DUST_DEFAULTS)
+            d.update(dust)
+            if spaxel_area is None:
+                raise ValueError("dust extinction needs the spaxel area (kpc^2)")
+            self.dust = d
+            self.spaxel_area = float(spaxel_area)
+            self.dust_exponent = _dev(dust_host.extinction_exponent(
+                self.wave_t.cpu().numpy(), d["extinction_model"], d["Rv"]), self.device)
+            self.dgr_params, self.dgr_broken = dust_host.dust_to_gas_params(
+                d["dust_to_gas_model"], d["Xco"])
+            self.ext_scale = dust_host.extinction_scale(d["dust_grain_density"])
 
     @classmethod
-    def from_workload(cls, w, device="cuda", psf=True, lsf=True):
+    def from_workload(cls, w, device="cuda", psf=True, lsf=True, dust=None):
+        area = None
+        if dust is not None:
+            from .synth import WORKLOADS
+
+            _, size = tel.spatial_bin_edges(WORKLOADS[w.name]["fov"], w.sbin, w.dist_z)
+            area = float(np.float32(size) ** 2)
         return cls(w.ssp.age, w.ssp.metallicity, w.ssp.wavelength, w.ssp.flux, w.wave_t, w.edges,
                    w.sbin, w.dist_z,
                    psf_taps=tel.gaussian_taps_1d(w.psf_size, w.psf_sigma) if psf else None,
                    lsf_taps=tel.lsf_taps(w.lsf_sigma, w.wave_res) if lsf else None,
-                   device=device, noise_s2n=getattr(w, "noise_s2n", None))
+                   device=device, noise_s2n=getattr(w, "noise_s2n", None), dust=dust,
+                   spaxel_area=area)
 
     # -------------------------------------------------------------- steps
     def assign(self, coords):
@@ -99,15 +124,35 @@ class IFURenderer:
     def sort(self, idx, mask=None):
         return ops.spaxel_sort(idx, self.sbin * self.sbin, mask)
 
+    def dust_av(self, star_coords, star_idx, gas_coords, gas_mass, gas_metals):
+        """A_V of every star from the gas (rubix's calculate_extinction): gas outside the
+        aperture has zero mass (filter_particles), per-cell extinction from
+        12 + log(O/H), cumulative column along z per spaxel, interpolated at the stars."""
+        if self.dust is None:
+            raise ValueError("this renderer has no dust configuration")
+        gc = _dev(gas_coords, self.device)
+        gm = _dev(gas_mass, self.device)
+        gidx = ops.spaxel_assign(gc, self.edges)
+        if self.apply_filter:
+            gm = ops.mask_zero_(gm.clone(), ops.aperture_mask(gc, self.edges))
+        gext = ops.dust_gas_extinction(gm, _dev(gas_metals, self.device), self.dgr_params,
+                                       self.dgr_broken, self.ext_scale, self.spaxel_area)
+        nb = int(self.edges.numel()) - 1
+        nseg = self.sbin * self.sbin
+        return ops.dust_av(gc, gidx, gext, _dev(star_coords, self.device), star_idx, nseg,
+                           max(nb * nb, nseg))
+
     def accumulate(self, mass, metallicity, age, velocity, perm, seg_offsets, out=None,
-                   with_lsf=False):
-        """Fused lookup/mass/Doppler/resample/sum; ``with_lsf`` adds the LSF epilogue."""
+                   with_lsf=False, dust_av=None):
+        """Fused lookup/mass/Doppler/resample/sum; ``with_lsf`` adds the LSF epilogue and
+        ``dust_av`` (A_V per particle) the dust transmission of each spectrum."""
         cube = ops.cube_forward(self.ssp_flux, self.ssp_metallicity, self.ssp_age, self.ssp_wave_z,
                                 self.wave_t, _dev(mass, self.device), _dev(metallicity, self.device),
                                 _dev(age, self.device), _dev(velocity, self.device),
                                 self.velocity_axis, perm, seg_offsets, self.sbin * self.sbin, out=out,
                                 lsf_taps=self.lsf_taps if with_lsf else None,
-                                lsf_crop=self.lsf_crop)
+                                lsf_crop=self.lsf_crop, dust_av=dust_av,
+                                dust_exponent=None if dust_av is None else self.dust_exponent)
         return cube.view(self.sbin, self.sbin, self.n_wave_t)
 
     def psf(self, cube, out=None):
@@ -123,14 +168,20 @@ class IFURenderer:
         return cube
 
     # -------------------------------------------------------------- whole path
-    def render(self, coords, velocity, mass, metallicity, age, fuse_lsf=True) -> CubeStages:
+    def render(self, coords, velocity, mass, metallicity, age, fuse_lsf=True,
+               gas=None) -> CubeStages:
         """Whole path.  With ``fuse_lsf`` the LSF runs inside the accumulate kernel and the
         PSF afterwards (the two act on different axes and commute), saving one read and
-        one write of the cube; the final cube is the same."""
+        one write of the cube; the final cube is the same.  ``gas`` = (coords, mass,
+        metals) applies the dust extinction of a renderer built with ``dust``."""
         idx, mask = self.assign(coords)
         perm, offs = self.sort(idx, mask)
+        av = None
+        if gas is not None:
+            av = self.dust_av(coords, idx, *gas)
         fuse = fuse_lsf and self.lsf_taps is not None
-        cube = self.accumulate(mass, metallicity, age, velocity, perm, offs, with_lsf=fuse)
+        cube = self.accumulate(mass, metallicity, age, velocity, perm, offs, with_lsf=fuse,
+                               dust_av=av)
         if fuse:
             c_psf = self.psf(cube) if self.psf_taps is not None else None
             final = c_psf if c_psf is not None else cube

@@ -249,3 +249,33 @@ def test_dusty_gordon23():
                              w.ssp.wavelength, w.dist_z, w.wave_t, apply_filter=False,
                              transmission=T)["cube"]
     assert_cube_close(cube.cpu().numpy().reshape(ref.shape), ref, what="Gordon23 dusty cube")
+
+
+def test_renderer_dust_matches_oracle():
+    """IFURenderer.render(gas=...) (the bench's path) against the oracle, no rotation."""
+    from rubix_gb300 import synth
+    from rubix_gb300 import telescope as tel
+    from rubix_gb300.api import IFURenderer
+
+    w = workload("small", n=4000)
+    g, _ = _gas(3000, seed=8)
+    rnd = IFURenderer.from_workload(w, device="cuda", dust={"extinction_model": "Gordon23",
+                                                            "Rv": 2.7})
+    p = w.particles
+    st = rnd.render(p.coords, p.velocity, p.mass, p.metallicity, p.age,
+                    gas=(g.coords, g.mass, g.metals))
+    _, size = tel.spatial_bin_edges(synth.WORKLOADS["small"]["fov"], w.sbin, w.dist_z)
+    area = float(np.float32(size) ** 2)
+    _, gf = oracle.filter_particles(g.coords, w.edges, mass=g.mass)
+    gext = do.gas_extinction(gf["mass"], g.metals, area)
+    gpa = oracle.square_spaxel_assignment(g.coords, w.edges)
+    spa = oracle.square_spaxel_assignment(p.coords, w.edges)
+    av = do.spaxel_av(g.coords[:, 2], gpa, gext, p.coords[:, 2], spa, w.sbin * w.sbin)
+    wave_um = (np.asarray(w.wave_t, np.float32) / np.float32(1e4)).astype(np.float64)
+    T = do.extinguish(do.gordon23(wave_um, 2.7), av)
+    ref = oracle.render_cube(p.coords, p.velocity, p.mass, p.metallicity, p.age, w.edges,
+                             w.sbin, w.ssp.metallicity, w.ssp.age, w.ssp.flux,
+                             w.ssp.wavelength, w.dist_z, w.wave_t, psf_size=w.psf_size,
+                             psf_sigma=w.psf_sigma, lsf_sigma=w.lsf_sigma,
+                             wave_res=w.wave_res, transmission=T)
+    assert_cube_close(st.final.cpu().numpy(), ref["final"], what="renderer dusty cube")
