@@ -196,3 +196,89 @@ class IFURenderer:
             final = cube.clone()  # keep the accumulate stage noise-free
         final = self.noise_(final)
         return CubeStages(idx, mask, perm, offs, cube, c_psf, c_lsf, False, final)
+
+    def host_stream(self, n_slots: int = 2) -> "HostStream":
+        """A ``HostStream`` rendering pinned host inputs into pinned host outputs with
+        the copies of one render overlapped with the compute of the next."""
+        return HostStream(self, n_slots)
+
+
+class HostStream:
+    """Back-to-back renders from host to host with overlapped transfers.
+
+    Each ``submit`` copies one galaxy's particle arrays from (pinned) host memory to a
+    device slot on an upload stream, renders it on the caller's current stream into
+    the slot's cube buffers, and copies the final cube to the given (pinned) host
+    tensor on a download stream.  Slots rotate, so the download of render k and the
+    upload of render k+1 run while render k+1 / k computes; events order the three
+    streams and keep a slot from being overwritten before its download ended.
+    ``synchronize`` makes the current stream wait for every download.
+    """
+
+    def __init__(self, renderer: IFURenderer, n_slots: int = 2):
+        self.r = renderer
+        dev = renderer.device
+        self.up = torch.cuda.Stream(dev)
+        self.down = torch.cuda.Stream(dev)
+        self.slots = [dict(inputs=None, cube=None, final=None,
+                           computed=torch.cuda.Event(), downloaded=torch.cuda.Event(),
+                           uploaded=torch.cuda.Event(), used=False)
+                      for _ in range(max(1, int(n_slots)))]
+        self.k = 0
+
+    def submit(self, coords, velocity, mass, metallicity, age, out: torch.Tensor) -> None:
+        r = self.r
+        slot = self.slots[self.k % len(self.slots)]
+        self.k += 1
+        host = (coords, velocity, mass, metallicity, age)
+        compute = torch.cuda.current_stream(r.device)
+        fresh = slot["inputs"] is None or any(d.shape != torch.Size(np.shape(h))
+                                              for d, h in zip(slot["inputs"], host))
+        if fresh:
+            slot["inputs"] = [torch.empty(tuple(np.shape(h)), dtype=torch.float32,
+                                          device=r.device) for h in host]
+        # upload: after the compute that last read this slot's inputs; into fresh
+        # buffers only after everything already on the compute stream, which may still
+        # use the recycled memory
+        if slot["used"] and not fresh:
+            self.up.wait_event(slot["computed"])
+        else:
+            self.up.wait_stream(compute)
+        with torch.cuda.stream(self.up):
+            for d, h in zip(slot["inputs"], host):
+                d.copy_(torch.as_tensor(h), non_blocking=True)
+            slot["uploaded"].record(self.up)
+        compute.wait_event(slot["uploaded"])
+        if slot["used"]:
+            compute.wait_event(slot["downloaded"])  # cube buffers free again
+        c, v, m, z, a = slot["inputs"]
+        idx, mask = r.assign(c)
+        perm, offs = r.sort(idx, mask)
+        fuse = r.lsf_taps is not None
+        if slot["cube"] is None:
+            L = r.n_wave_t
+            slot["cube"] = torch.empty((r.sbin * r.sbin, L), dtype=torch.float32,
+                                       device=r.device)
+            slot["final"] = torch.empty((r.sbin, r.sbin, L), dtype=torch.float32,
+                                        device=r.device)
+        cube = r.accumulate(m, z, a, v, perm, offs, out=slot["cube"], with_lsf=fuse)
+        if r.psf_taps is not None:
+            final = r.psf(cube, out=slot["final"])
+        else:
+            slot["final"].copy_(cube)
+            final = slot["final"]
+        if not fuse and r.lsf_taps is not None:
+            final = slot["final"].copy_(r.lsf(final))
+        r.noise_(final)
+        slot["computed"].record(compute)
+        self.down.wait_event(slot["computed"])
+        with torch.cuda.stream(self.down):
+            out.copy_(final, non_blocking=True)
+            slot["downloaded"].record(self.down)
+        slot["used"] = True
+
+    def synchronize(self) -> None:
+        """The current stream waits for every upload and download issued so far."""
+        compute = torch.cuda.current_stream(self.r.device)
+        compute.wait_stream(self.up)
+        compute.wait_stream(self.down)

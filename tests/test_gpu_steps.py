@@ -185,3 +185,29 @@ def test_known_answers_on_gpu():
     want = oracle.apply_psf(c, np.ones((3, 3)))
     np.testing.assert_allclose(o, want, atol=1e-6)
     torch.cuda.synchronize()
+
+
+def test_host_stream_matches_render():
+    """IFURenderer.host_stream (overlapped upload / compute / download over two slots)
+    gives every submitted galaxy the cube of a plain render."""
+    import torch
+
+    from rubix_gb300.api import IFURenderer
+
+    ws = [workload("small", n=3000 + 500 * k) for k in range(3)]
+    rnd = IFURenderer.from_workload(ws[0], device="cuda")
+    hs = rnd.host_stream(2)
+    outs = []
+    for k in range(5):
+        p = ws[k % 3].particles
+        h = [torch.from_numpy(a).pin_memory() for a in (p.coords, p.velocity, p.mass,
+                                                        p.metallicity, p.age)]
+        o = torch.empty((ws[0].sbin, ws[0].sbin, ws[0].wave_t.size)).pin_memory()
+        hs.submit(*h, out=o)
+        outs.append(o)
+    hs.synchronize()
+    torch.cuda.synchronize()
+    for k in range(5):
+        p = ws[k % 3].particles
+        ref = rnd.render(p.coords, p.velocity, p.mass, p.metallicity, p.age).final.cpu()
+        assert torch.equal(outs[k], ref), f"galaxy {k}"
