@@ -168,6 +168,25 @@ RUBIX_API int rubix_cube_fwd_dust(const float* ssp_flux, const float* ssp_metall
                                   size_t workspace_bytes, void* stream);
 
 /*
+ * The adjoint of rubix_cube_fwd_dust for the particle inputs (what jax.grad through
+ * calculate_extinction gives for mass, metallicity, age and velocity; A_V, a function
+ * of the coordinates and the gas, is held fixed): rubix_cube_bwd with the cube
+ * adjoint seen through each particle's transmission 2^(ext_exponent[t] * av[i]).
+ * Same workspace (rubix_cube_bwd_workspace_size) and limits as rubix_cube_bwd.
+ */
+RUBIX_API int rubix_cube_bwd_dust(const float* ssp_flux, const float* ssp_metallicity,
+                                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                                  int32_t n_age, int32_t n_wave, const float* wave_t,
+                                  int32_t n_wave_t, const float* mass, const float* metallicity,
+                                  const float* age, const float* velocity, int64_t vel_stride,
+                                  int32_t vel_component, const float* av,
+                                  const float* ext_exponent, const int32_t* perm,
+                                  const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                  const float* adj, int64_t adj_stride, float* grad_mass,
+                                  float* grad_metallicity, float* grad_age, float* grad_vlos,
+                                  void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Replaces the per-cell extinction of rubix/spectra/dust/dust_extinction.py:291-306
  * (12 + log10(O/(16 H)), calculate_dust_to_gas_ratio :13-90, calculate_extinction
  * :93-160, divided by the spaxel area).

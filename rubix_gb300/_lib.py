@@ -84,6 +84,14 @@ SIGNATURES = {
          _vp, _i64, _vp, _vp, _vp, _vp,
          _vp, _sz, _vp],
     ),
+    "rubix_cube_bwd_dust": (
+        _c.c_int,
+        [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32,
+         _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp,
+         _vp, _vp, _i32, _i64,
+         _vp, _i64, _vp, _vp, _vp, _vp,
+         _vp, _sz, _vp],
+    ),
     "rubix_ragged_assign": (_c.c_int, [_vp, _i64, _i64, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _vp]),
     "rubix_ragged_psf_fwd": (_c.c_int, [_vp, _vp, _i32, _i64, _i64, _i32, _vp, _vp, _vp, _i32,

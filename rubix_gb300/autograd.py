@@ -15,7 +15,10 @@ CUDA kernels:
               dL/dsigma_lsf = <gP, LSF_{dt}(A)>
 
 The PSF and LSF act on different axes and commute, so the forward cube equals
-rubix's convolve_psf followed by convolve_lsf.  Gradients flow to the particle
+rubix's convolve_psf followed by convolve_lsf.  With ``dust_av`` / ``dust_exponent``
+(calc_dusty_ifu's calculate_extinction) every particle's spectrum carries its dust
+transmission in both passes; A_V itself is held fixed (no gradient to the coordinates
+or the gas).  Gradients flow to the particle
 inputs (velocity: the line-of-sight component only) and to ``sigma_psf`` /
 ``sigma_lsf`` given as tensors; the spaxel assignment (coordinates) is piecewise
 constant and gets none, as in rubix.
@@ -75,12 +78,13 @@ class DatacubeFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, mass, metallicity, age, velocity, sigma_psf, sigma_lsf, renderer, perm,
-                seg_offsets, psf_size, wave_res):
+                seg_offsets, psf_size, wave_res, dust_av=None):
         r = renderer
         nseg = r.sbin * r.sbin
+        dust_e = None if dust_av is None else r.dust_exponent
         A = ops.cube_forward(r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t,
                              mass, metallicity, age, velocity, r.velocity_axis, perm,
-                             seg_offsets, nseg)
+                             seg_offsets, nseg, dust_av=dust_av, dust_exponent=dust_e)
         sp, sl = _scalar(sigma_psf), _scalar(sigma_lsf)
         tl, _ = lsf_taps_grad(sl, wave_res)
         crop = (tl.size - 1) // 2
@@ -90,6 +94,7 @@ class DatacubeFunction(torch.autograd.Function):
         ctx.save_for_backward(mass, metallicity, age, velocity, A, Q)
         ctx.r = r
         ctx.perm, ctx.seg_offsets = perm, seg_offsets
+        ctx.dust = (dust_av, dust_e)
         ctx.sp, ctx.sl, ctx.psf_size, ctx.wave_res = sp, sl, int(psf_size), wave_res
         ctx.sigma_dtypes = (
             sigma_psf.dtype if isinstance(sigma_psf, torch.Tensor) else None,
@@ -107,13 +112,13 @@ class DatacubeFunction(torch.autograd.Function):
         crop = (tl.size - 1) // 2
         gP = ops.psf_forward(g, _psf_adjoint_taps(tp))
         need = ctx.needs_input_grad
-        grads = [None] * 11
+        grads = [None] * 12
         if any(need[:4]):
             h = ops.lsf_forward(gP, tl[::-1].copy(), tl.size - 1 - crop)
             gm, gz, ga, gv = ops.cube_backward(
                 r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t, mass,
                 metallicity, age, velocity, r.velocity_axis, ctx.perm, ctx.seg_offsets, nseg,
-                h.view(nseg, -1))
+                h.view(nseg, -1), dust_av=ctx.dust[0], dust_exponent=ctx.dust[1])
             grads[0] = gm.view_as(mass).to(mass.dtype) if need[0] else None
             grads[1] = gz.view_as(metallicity).to(metallicity.dtype) if need[1] else None
             grads[2] = ga.view_as(age).to(age.dtype) if need[2] else None
@@ -135,11 +140,17 @@ class DatacubeFunction(torch.autograd.Function):
 
 
 def render_cube(renderer, coords, velocity, mass, metallicity, age, sigma_psf, sigma_lsf,
-                psf_size: int, wave_res: float):
+                psf_size: int, wave_res: float, gas=None):
     """Differentiable datacube of one galaxy: aperture filter, spaxel sort (no
     gradient) and ``DatacubeFunction``.  All particle tensors must be CUDA tensors;
-    ``sigma_psf`` / ``sigma_lsf`` are tensors (or floats when no gradient is wanted)."""
+    ``sigma_psf`` / ``sigma_lsf`` are tensors (or floats when no gradient is wanted).
+    ``gas`` = (coords, mass, metals) with a renderer built with ``dust`` applies the dust
+    extinction (A_V computed once, without gradient)."""
     idx, mask = renderer.assign(coords)
     perm, offs = renderer.sort(idx, mask)
+    av = None
+    if gas is not None:
+        with torch.no_grad():
+            av = renderer.dust_av(coords, idx, *gas)
     return DatacubeFunction.apply(mass, metallicity, age, velocity, sigma_psf, sigma_lsf,
-                                  renderer, perm, offs, psf_size, wave_res)
+                                  renderer, perm, offs, psf_size, wave_res, av)

@@ -52,6 +52,7 @@ struct AdjArgs {
   const int2* bucket;
   int row_cap;
   int chunk;
+  const float* dust_e2;  // per telescope wavelength: -0.4 log2(10) A(lambda)/A(V)
 };
 
 struct AdjSmem {
@@ -169,13 +170,17 @@ __device__ __forceinline__ void walk_step2(float x, unsigned& aa, unsigned& ab, 
       : "memory");
 }
 
-// The 8 partial sums of one particle over this thread's R wavelengths.
-template <int R, bool kGeneric>
+// The 8 partial sums of one particle over this thread's R wavelengths.  With kDust the
+// cube adjoint h_t is seen through the particle's dust transmission 2^(e_t A_V): the
+// particle adds beta g_t I_t to the cube, so every sum against h takes h_t g_t.
+template <int R, bool kGeneric, bool kDust>
 __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
                                          const float4* __restrict__ rb, int ks, int ke, float B,
                                          float A0, const int2* __restrict__ s_bucket,
                                          const float (&lam)[R], const float (&dlam)[R],
-                                         const float (&h)[R], float (&s)[kAdjSums]) {
+                                         const float (&h)[R], float (&s)[kAdjSums],
+                                         const float* __restrict__ e2, float av, int t0,
+                                         int n_t) {
   const float u = A0 - B;
   int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
   b = min(max(b, 0), kBuckets - 1);
@@ -207,14 +212,16 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
     const float I = fmaf(d, e.y, e.z);
     const float IZ = fmaf(d, f.y, f.x);
     const float IA = fmaf(d, f.w, f.z);
-    s[0] = fmaf(h[r], I, s[0]);
+    float hr = h[r];
+    if constexpr (kDust) hr = __fmul_rn(hr, exp2f(__fmul_rn(__ldg(e2 + min(t0 + r, n_t - 1)), av)));
+    s[0] = fmaf(hr, I, s[0]);
     s[1] = fmaf(dlam[r], I, s[1]);
-    s[2] = fmaf(h[r], IZ, s[2]);
+    s[2] = fmaf(hr, IZ, s[2]);
     s[3] = fmaf(dlam[r], IZ, s[3]);
-    s[4] = fmaf(h[r], IA, s[4]);
+    s[4] = fmaf(hr, IA, s[4]);
     s[5] = fmaf(dlam[r], IA, s[5]);
     const float xs = x * e.y;  // lambda_t * slope
-    s[6] = fmaf(h[r], xs, s[6]);
+    s[6] = fmaf(hr, xs, s[6]);
     s[7] = fmaf(dlam[r], xs, s[7]);
   }
 }
@@ -246,7 +253,7 @@ __device__ __forceinline__ float warp_reduce8(const float (&v)[8], int lane) {
   return d;
 }
 
-template <int R>
+template <int R, bool kDust>
 __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const AdjSmem SL = adj_smem_layout(a.n_wave, a.nZ + a.nA, a.row_cap);
@@ -323,12 +330,13 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
       const int4 rb = rec.b;
       const int ks = rb.y, ke = rb.z & ~kGenericFlag;
       float sums[kAdjSums];
+      const float av = kDust ? rec.c.w : 0.f;
       if (rb.z & kGenericFlag)
-        adj_eval<R, true>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h,
-                          sums);
+        adj_eval<R, true, kDust>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam,
+                                 h, sums, a.dust_e2, av, t0, n_t);
       else
-        adj_eval<R, false>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam, h,
-                           sums);
+        adj_eval<R, false, kDust>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam,
+                                  dlam, h, sums, a.dust_e2, av, t0, n_t);
       const float wv = warp_reduce8(sums, lane);
       if ((lane & 3) == 0) {
         const int v = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
@@ -372,23 +380,29 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
   }
 }
 
-template <int R>
-int launch_adjoint(const AdjArgs& args, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(cube_adjoint_kernel<R>,
+template <int R, bool kDust>
+int launch_adjoint_t(const AdjArgs& args, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(cube_adjoint_kernel<R, kDust>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess)
     return set_error(RUBIX_E_CUDA, "cudaFuncSetAttribute(cube_adjoint_kernel): %s",
                      cudaGetErrorString(e));
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_adjoint_kernel<R>, kAdjThreads,
-                                                    smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_adjoint_kernel<R, kDust>,
+                                                    kAdjThreads, smem);
   if (e != cudaSuccess || per_sm < 1)
     return set_error(RUBIX_E_UNSUPPORTED,
                      "cube_adjoint_kernel does not fit on an SM with %zu bytes of shared memory",
                      smem);
-  cube_adjoint_kernel<R><<<sm_count() * per_sm, kAdjThreads, smem, st>>>(args);
+  cube_adjoint_kernel<R, kDust><<<sm_count() * per_sm, kAdjThreads, smem, st>>>(args);
   RUBIX_LAUNCH_CHECK("cube_adjoint_kernel");
   return RUBIX_OK;
+}
+
+template <int R>
+int launch_adjoint(const AdjArgs& args, size_t smem, cudaStream_t st) {
+  return args.dust_e2 ? launch_adjoint_t<R, true>(args, smem, st)
+                      : launch_adjoint_t<R, false>(args, smem, st);
 }
 
 }  // namespace
@@ -404,26 +418,28 @@ extern "C" size_t rubix_cube_bwd_workspace_size(int64_t n, int32_t n_segments, i
       .bytes;
 }
 
-extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicity,
-                              const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
-                              int32_t n_age, int32_t n_wave, const float* wave_t,
-                              int32_t n_wave_t, const float* mass, const float* metallicity,
-                              const float* age, const float* velocity, int64_t vel_stride,
-                              int32_t vel_component, const int32_t* perm,
-                              const int32_t* seg_offsets, int32_t n_segments, int64_t n,
-                              const float* adj, int64_t adj_stride, float* grad_mass,
-                              float* grad_metallicity, float* grad_age, float* grad_vlos,
-                              void* workspace, size_t workspace_bytes, void* stream) {
-  RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "rubix_cube_bwd: bad n");
-  RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "rubix_cube_bwd: n_segments < 0");
+namespace rubix {
+namespace {
+
+int cube_bwd_impl(const char* who, const float* ssp_flux, const float* ssp_metallicity,
+                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met, int32_t n_age,
+                  int32_t n_wave, const float* wave_t, int32_t n_wave_t, const float* mass,
+                  const float* metallicity, const float* age, const float* velocity,
+                  int64_t vel_stride, int32_t vel_component, const float* av,
+                  const float* dust_e2, const int32_t* perm, const int32_t* seg_offsets,
+                  int32_t n_segments, int64_t n, const float* adj, int64_t adj_stride,
+                  float* grad_mass, float* grad_metallicity, float* grad_age, float* grad_vlos,
+                  void* workspace, size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "%s: bad n", who);
+  RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "%s: n_segments < 0", who);
   RUBIX_REQUIRE(n_met >= 2 && n_age >= 2, RUBIX_E_SHAPE,
-                "rubix_cube_bwd: SSP grid needs >= 2 metallicities and >= 2 ages");
-  RUBIX_REQUIRE(n_wave >= 2, RUBIX_E_SHAPE, "rubix_cube_bwd: SSP grid needs >= 2 wavelengths");
+                "%s: SSP grid needs >= 2 metallicities and >= 2 ages", who);
+  RUBIX_REQUIRE(n_wave >= 2, RUBIX_E_SHAPE, "%s: SSP grid needs >= 2 wavelengths", who);
   RUBIX_REQUIRE(n_wave_t >= 1 && n_wave_t <= kMaxWaveT, RUBIX_E_SHAPE,
-                "rubix_cube_bwd: n_wave_t must be in [1, %d], got %d", kMaxWaveT, n_wave_t);
-  RUBIX_REQUIRE(adj_stride >= n_wave_t, RUBIX_E_SHAPE, "rubix_cube_bwd: adj_stride < n_wave_t");
+                "%s: n_wave_t must be in [1, %d], got %d", who, kMaxWaveT, n_wave_t);
+  RUBIX_REQUIRE(adj_stride >= n_wave_t, RUBIX_E_SHAPE, "%s: adj_stride < n_wave_t", who);
   RUBIX_REQUIRE(vel_component >= 0 && vel_component < vel_stride, RUBIX_E_INVALID,
-                "rubix_cube_bwd: vel_component outside the velocity row");
+                "%s: vel_component outside the velocity row", who);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // every gradient entry is written: zeros for particles outside the sorted set
   float* grads[4] = {grad_mass, grad_metallicity, grad_age, grad_vlos};
@@ -432,25 +448,25 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
   if (n_segments == 0 || n == 0) return RUBIX_OK;
   RUBIX_REQUIRE(ssp_flux && ssp_metallicity && ssp_age && ssp_wave_z && wave_t && seg_offsets &&
                     adj && mass && metallicity && age && velocity && perm,
-                RUBIX_E_INVALID, "rubix_cube_bwd: null pointer");
+                RUBIX_E_INVALID, "%s: null pointer", who);
   const size_t need = rubix_cube_bwd_workspace_size(n, n_segments, n_wave_t, n_met, n_age, n_wave);
   RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
-                "rubix_cube_bwd: workspace of %zu bytes needed, %zu given", need, workspace_bytes);
+                "%s: workspace of %zu bytes needed, %zu given", who, need, workspace_bytes);
   RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
-                "rubix_cube_bwd: workspace must be 256-byte aligned");
+                "%s: workspace must be 256-byte aligned", who);
   const int row_cap = n_wave + 2;
   const AdjSmem SL = adj_smem_layout(n_wave, n_met + n_age, row_cap);
   RUBIX_REQUIRE(SL.total <= 227 * 1024, RUBIX_E_UNSUPPORTED,
-                "rubix_cube_bwd: SSP grid of %d wavelengths needs %zu bytes of shared memory "
+                "%s: SSP grid of %d wavelengths needs %zu bytes of shared memory "
                 "(limit 232448)",
-                n_wave, SL.total);
+                who, n_wave, SL.total);
 
   const CubeTuning tune = cube_tuning_current();
   const CubeLayout L =
       carve_cube(workspace, n, n_segments, n_wave_t, n_met, n_age, n_wave, tune.chunk);
   const CubeInputs in{ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met, n_age, n_wave,
                       wave_t, n_wave_t, mass, metallicity, age, velocity, vel_stride,
-                      vel_component, perm, seg_offsets, n_segments, n};
+                      vel_component, perm, seg_offsets, n_segments, n, av};
   {
     const int rc = cube_prepare(in, L, tune, /*with_grad=*/true, st);
     if (rc != RUBIX_OK) return rc;
@@ -480,6 +496,7 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
   args.bucket = L.bucket;
   args.row_cap = row_cap;
   args.chunk = tune.chunk;
+  args.dust_e2 = dust_e2;
   const int need_r = (n_wave_t + kAdjThreads - 1) / kAdjThreads;
   const size_t smem = SL.total;
   if (need_r <= 1) return launch_adjoint<1>(args, smem, st);
@@ -489,4 +506,44 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
   if (need_r <= 8) return launch_adjoint<8>(args, smem, st);
   if (need_r <= 10) return launch_adjoint<10>(args, smem, st);
   return launch_adjoint<11>(args, smem, st);  // kAdjThreads * 11 >= kMaxWaveT
+}
+
+}  // namespace
+}  // namespace rubix
+
+extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicity,
+                              const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                              int32_t n_age, int32_t n_wave, const float* wave_t,
+                              int32_t n_wave_t, const float* mass, const float* metallicity,
+                              const float* age, const float* velocity, int64_t vel_stride,
+                              int32_t vel_component, const int32_t* perm,
+                              const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                              const float* adj, int64_t adj_stride, float* grad_mass,
+                              float* grad_metallicity, float* grad_age, float* grad_vlos,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  return cube_bwd_impl("rubix_cube_bwd", ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met,
+                       n_age, n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity,
+                       vel_stride, vel_component, nullptr, nullptr, perm, seg_offsets,
+                       n_segments, n, adj, adj_stride, grad_mass, grad_metallicity, grad_age,
+                       grad_vlos, workspace, workspace_bytes, stream);
+}
+
+extern "C" int rubix_cube_bwd_dust(const float* ssp_flux, const float* ssp_metallicity,
+                                   const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                                   int32_t n_age, int32_t n_wave, const float* wave_t,
+                                   int32_t n_wave_t, const float* mass, const float* metallicity,
+                                   const float* age, const float* velocity, int64_t vel_stride,
+                                   int32_t vel_component, const float* av,
+                                   const float* ext_exponent, const int32_t* perm,
+                                   const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                   const float* adj, int64_t adj_stride, float* grad_mass,
+                                   float* grad_metallicity, float* grad_age, float* grad_vlos,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(ext_exponent != nullptr && (n == 0 || av != nullptr), RUBIX_E_INVALID,
+                "rubix_cube_bwd_dust: null A_V or extinction exponent");
+  return cube_bwd_impl("rubix_cube_bwd_dust", ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z,
+                       n_met, n_age, n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity,
+                       vel_stride, vel_component, av, ext_exponent, perm, seg_offsets,
+                       n_segments, n, adj, adj_stride, grad_mass, grad_metallicity, grad_age,
+                       grad_vlos, workspace, workspace_bytes, stream);
 }

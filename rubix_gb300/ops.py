@@ -194,10 +194,12 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
 
 
 def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, metallicity,
-                  age, velocity, vel_component, perm, seg_offsets, n_segments, adj):
+                  age, velocity, vel_component, perm, seg_offsets, n_segments, adj,
+                  dust_av=None, dust_exponent=None):
     """Gradients (mass, metallicity, age, v_los) of <adj, cube> with cube the output of
-    ``cube_forward`` without LSF; ``adj`` is [n_segments, >=L].  Four [n] tensors, zero
-    for particles outside the sorted set."""
+    ``cube_forward`` without LSF (with the same ``dust_av`` / ``dust_exponent``, A_V held
+    fixed); ``adj`` is [n_segments, >=L].  Four [n] tensors, zero for particles outside
+    the sorted set."""
     ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
     nz, na, nw = ssp_flux.shape
     ssp_metallicity = _contig("ssp_metallicity", ssp_metallicity, torch.float32)
@@ -222,11 +224,25 @@ def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, 
     grads = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(4)]
     nbytes = _lib.query("rubix_cube_bwd_workspace_size", n, int(n_segments), L, nz, na, nw)
     ws = workspace(nbytes, dev)
-    _lib.call("rubix_cube_bwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
-              _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
-              _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
-              _ptr(seg_offsets), int(n_segments), n, _ptr(adj), adj.stride(0),
-              *[_ptr(g) for g in grads], _ptr(ws), ws.numel(), _stream(dev))
+    if (dust_av is None) != (dust_exponent is None):
+        raise ValueError("dust_av and dust_exponent go together")
+    if dust_av is None:
+        _lib.call("rubix_cube_bwd", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
+                  _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
+                  _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(perm),
+                  _ptr(seg_offsets), int(n_segments), n, _ptr(adj), adj.stride(0),
+                  *[_ptr(g) for g in grads], _ptr(ws), ws.numel(), _stream(dev))
+    else:
+        dust_av = _contig("dust_av", dust_av, torch.float32).reshape(-1)
+        dust_exponent = _contig("dust_exponent", dust_exponent, torch.float32).reshape(-1)
+        if dust_av.numel() != n or dust_exponent.numel() != L:
+            raise ValueError("dust_av must be [n] and dust_exponent [L]")
+        _lib.call("rubix_cube_bwd_dust", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
+                  _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
+                  _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(dust_av),
+                  _ptr(dust_exponent), _ptr(perm), _ptr(seg_offsets), int(n_segments), n,
+                  _ptr(adj), adj.stride(0), *[_ptr(g) for g in grads], _ptr(ws), ws.numel(),
+                  _stream(dev))
     # setup, corner table, prefix, count, scans (one launch), fill, adjoint (+ gather)
     _count((7 + (1 if n > 0 else 0)) if (n_segments > 0 and n > 0) else 0)
     return tuple(grads)
