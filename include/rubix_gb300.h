@@ -234,6 +234,15 @@ RUBIX_API int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const i
                             void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * Replaces the array preparation of rubix/core/fits.py:88-100 (astropy writing
+ * datacube.T as a float32 image HDU): out[(l*B + b)*A + a] = the big-endian bit
+ * pattern of cube[(a*B + b)*spaxel_stride + l] for a < A, b < B (B <= 65535), l < L,
+ * i.e. the bytes of the FITS data array of the cube [A][B][L].
+ */
+RUBIX_API int rubix_fits_cube_layout(const float* cube, int32_t A, int32_t B, int32_t L,
+                                     int64_t spaxel_stride, void* out, void* stream);
+
+/*
  * No counterpart in rubix (rubix has no C interface; JAX allocates its buffers).
  *
  * rubix_cube_fwd without the workspace argument, for callers that cannot allocate

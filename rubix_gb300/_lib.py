@@ -55,6 +55,7 @@ SIGNATURES = {
     "rubix_dust_gas_extinction": (_c.c_int, [_vp, _vp, _i64, _i32, _i32, _i64, _vp, _i32,
                                              _c.c_float, _c.c_float, _vp, _vp]),
     "rubix_dust_apply_rows": (_c.c_int, [_vp, _i64, _i32, _i64, _vp, _vp, _vp]),
+    "rubix_fits_cube_layout": (_c.c_int, [_vp, _i32, _i32, _i32, _i64, _vp, _vp]),
     "rubix_dust_av_workspace_size": (_sz, [_i64, _i32]),
     "rubix_dust_av": (_c.c_int, [_vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _i32,
                                  _vp, _vp, _sz, _vp]),

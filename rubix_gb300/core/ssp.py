@@ -1,19 +1,25 @@
 """SSP templates and their lookup (rubix/core/ssp.py:12-98, spectra/ssp/grid.py:22-124).
 
-rubix loads named templates from HDF5/FITS files (spectra/ssp/factory.py:13-76) that
-are not shipped with this package; templates are registered here instead, either as
-arrays (``register_ssp_template``) or from the seeded synthetic generator with the
-name ``"synthetic"`` (parameters under ``config["ssp"]["template"]``).
+rubix loads named templates from HDF5/FITS files (spectra/ssp/factory.py:13-76).  Here a
+template is, in order: a grid registered as arrays (``register_ssp_template``); the
+seeded synthetic generator (name ``"synthetic"``, parameters under
+``config["ssp"]["template"]``); or one of rubix's named templates read from its file in
+the template directory (``RUBIX_GB300_TEMPLATE_PATH``, default ``templates/`` next to
+this package).  Files in rubix's pyPipe3D FITS format (MaStar, .fits or .fits.gz) are
+read with the package's own FITS reader; HDF5 templates (BC03, FSPS) need h5py, which is
+not available, and are refused with that reason.  Nothing is downloaded.
 """
 
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass
 from typing import Callable, Dict
 
 import numpy as np
 import torch
 
+from .. import fits as fitsio
 from .. import ops, synth
 from ..logging import get_logger
 from .data import device_of, flat_particles, like_input
@@ -69,6 +75,105 @@ class SSPGrid:
 
 _TEMPLATES: Dict[str, SSPGrid] = {}
 
+# rubix/config/rubix_config.yml:136-240: the units the SSP grid is held in, and the
+# named templates with their file formats and field units
+SSP_UNITS = {"age": "Gyr", "metallicity": "", "wavelength": "Angstrom",
+             "flux": "Lsun/Angstrom"}
+_FIELDS = {k: {"name": k, "units": u, "in_log": False} for k, u in SSP_UNITS.items()}
+SSP_TEMPLATES = {
+    "BruzualCharlot2003": {"name": "Bruzual & Charlot (2003)", "format": "HDF5",
+                           "file_name": "BC03lr.h5", "fields": _FIELDS},
+    "Mastar_CB19_SLOG_1_5": {"name": "Mastar Charlot & Bruzual (2019)", "format": "PyPipe3D",
+                             "file_name": "MaStar_CB19.slog_1_5.fits.gz", "fields": _FIELDS},
+    "FSPS": {"name": "FSPS (Conroy et al. 2009)", "format": "fsps", "file_name": "fsps.h5",
+             "fields": dict(_FIELDS, age={"name": "age", "units": "Gyr", "in_log": True},
+                            metallicity={"name": "metallicity", "units": "",
+                                         "in_log": True})},
+}
+
+# unit factors to the internal units (the conversions rubix does with astropy units)
+_UNIT_FACTORS = {
+    "age": {"Gyr": 1.0, "Myr": 1e-3, "kyr": 1e-6, "yr": 1e-9},
+    "metallicity": {"": 1.0},
+    "wavelength": {"Angstrom": 1.0, "nm": 10.0, "um": 1e4, "micron": 1e4, "cm": 1e8, "m": 1e10},
+    "flux": {"Lsun/Angstrom": 1.0, "erg/s/Angstrom": 1.0 / 3.828e33,
+             "Lsun/nm": 0.1, "Lsun/um": 1e-4},
+}
+
+
+def template_path() -> str:
+    return os.environ.get("RUBIX_GB300_TEMPLATE_PATH",
+                          os.path.join(os.path.dirname(os.path.dirname(__file__)), "templates"))
+
+
+def convert_units(data, field: str, from_units: str) -> np.ndarray:
+    """grid.py:128-149 for the units of ``_UNIT_FACTORS`` (float32 result)."""
+    table = _UNIT_FACTORS[field]
+    if from_units not in table:
+        raise ValueError(f"cannot convert {field} from units {from_units!r} "
+                         f"(known: {sorted(table)})")
+    return (np.asarray(data, dtype=np.float64) * table[from_units]).astype(np.float32)
+
+
+def _pypipe3d_models(header, n_models: int):
+    """grid.py:466-515: ages (Gyr), metallicities and mass-to-light of each model from
+    the NAME<i> ("..._<age>[Gyr|Myr]_z<digits>...") and NORM<i> cards."""
+    ages = np.zeros(n_models, np.float32)
+    Zs = np.zeros(n_models, np.float32)
+    mtol = np.ones(n_models, np.float32)
+    for i in range(n_models):
+        parts = str(header[f"NAME{i}"]).split("_")[2:]
+        tok = parts[0]
+        mult = 1.0
+        if "yr" in tok:
+            mult = {"Gyr": 1.0, "Myr": 1.0 / 1000}[tok[-3:]]
+            tok = tok[:-3]
+        ages[i] = np.float32(mult * np.float32(tok))
+        Zs[i] = np.float32(parts[1].split(".")[0].replace("z", "0."))
+        norm = np.float32(header[f"NORM{i}"])
+        mtol[i] = np.float32(1) / norm if norm != 0 else np.float32(1)
+    return np.unique(ages), np.unique(Zs), mtol
+
+
+def load_pypipe3d(path: str, fields: dict = None) -> SSPGrid:
+    """pyPipe3DSSPGrid.from_file (grid.py:518-581): models along NAXIS2 (metallicity
+    major, then age), wavelengths CRVAL1 + CDELT1 (i + 1 - CRPIX1), flux divided by
+    each model's mass-to-light ratio, fields converted to the internal units."""
+    hdu = fitsio.read_fits(path)[0]
+    h = hdu.header
+    n_models = int(h["NAXIS2"])
+    ages, mets, m2l = _pypipe3d_models(h, n_models)
+    cdelt = h.get("CDELT1", 1) or 1
+    wave = (h["CRVAL1"] + cdelt * (np.arange(int(h["NAXIS1"])) + 1 - h["CRPIX1"]))
+    flux = (np.asarray(hdu.data, np.float32) / m2l[:, None]).astype(np.float32)
+    flux = flux.reshape(len(mets), len(ages), len(wave))
+    raw = {"flux": flux, "wavelength": wave, "age": ages, "metallicity": mets}
+    out = {}
+    for name, info in (fields or _FIELDS).items():
+        if name not in raw:
+            raise ValueError(f"Field {name} not recognized")
+        d = raw[name]
+        if info.get("in_log"):
+            d = np.power(10.0, np.asarray(d, np.float64))
+        out[name] = convert_units(d, name, info.get("units", SSP_UNITS[name]))
+    return SSPGrid(**out)
+
+
+def load_ssp_file(name: str) -> SSPGrid:
+    """spectra/ssp/factory.py:13-76 for the templates rubix names, from the template
+    directory."""
+    cfg = SSP_TEMPLATES[name]
+    path = os.path.join(template_path(), cfg["file_name"])
+    fmt = cfg["format"].lower()
+    if fmt in ("hdf5", "fsps"):
+        raise ValueError(f"SSP template {name} is an HDF5 file ({cfg['file_name']}); reading "
+                         "HDF5 needs h5py, which is not available")
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"SSP template file {path} not found (templates are not "
+                                "downloaded; place the file there or set "
+                                "RUBIX_GB300_TEMPLATE_PATH)")
+    return load_pypipe3d(path, cfg["fields"])
+
 
 def register_ssp_template(name: str, grid: SSPGrid) -> None:
     """Make ``grid`` available as ``config["ssp"]["template"]["name"] == name``."""
@@ -85,6 +190,10 @@ def get_ssp_template(name: str, params: dict | None = None) -> SSPGrid:
         p.update({k: v for k, v in (params or {}).items() if k in p})
         s = synth.make_ssp(p["n_age"], p["n_met"], p["n_wave"], seed=p["seed"])
         return SSPGrid(age=s.age, metallicity=s.metallicity, wavelength=s.wavelength, flux=s.flux)
+    if name in SSP_TEMPLATES:
+        grid = load_ssp_file(name)
+        _TEMPLATES[name] = grid
+        return grid
     raise ValueError(
         f"SSP template {name} is not available: register its grid with "
         "rubix_gb300.core.ssp.register_ssp_template (template files are not shipped)")
@@ -116,4 +225,5 @@ def get_lookup_interpolation(config: dict) -> Callable:
 
 
 __all__ = ["SSPGrid", "register_ssp_template", "get_ssp", "get_ssp_template",
-           "get_lookup_interpolation", "like_input"]
+           "get_lookup_interpolation", "like_input", "load_pypipe3d", "load_ssp_file",
+           "SSP_TEMPLATES", "SSP_UNITS", "convert_units", "template_path"]

@@ -29,6 +29,7 @@ __all__ = [
     "dust_gas_extinction",
     "dust_av",
     "dust_apply_rows_",
+    "fits_cube_layout",
     "workspace",
 ]
 
@@ -529,6 +530,21 @@ def dust_apply_rows_(rows: torch.Tensor, av, exponent) -> torch.Tensor:
               _ptr(exponent), _stream(rows.device))
     _count(1 if n * L > 0 else 0)
     return rows
+
+
+def fits_cube_layout(cube: torch.Tensor, out=None) -> torch.Tensor:
+    """cube [A, B, L] float32 -> int32 [L, B, A] holding big-endian float32 bit patterns
+    (the bytes of ``cube.T`` in a FITS file), ``rubix_fits_cube_layout``."""
+    _check_cuda("cube", cube, torch.float32)
+    if cube.dim() != 3 or cube.stride(2) != 1 or cube.stride(0) != cube.shape[1] * cube.stride(1):
+        cube = cube.contiguous()
+    A, B, L = (int(x) for x in cube.shape)
+    if out is None:
+        out = torch.empty((L, B, A), dtype=torch.int32, device=cube.device)
+    _lib.call("rubix_fits_cube_layout", _ptr(cube), A, B, L, cube.stride(1), _ptr(out),
+              _stream(cube.device))
+    _count(1 if A * B * L > 0 else 0)
+    return out
 
 
 def _key_passes(max_key: int) -> int:
