@@ -373,6 +373,20 @@ def dusty_bench(dev, w, d_in, steps, warmup, flush, n_gas=500_000):
                         "broken power-law dust-to-gas ratio (X_CO = Z)"}
 
 
+def fits_bench(dev, cube, steps, warmup, flush):
+    """FITS layout of the final cube (transpose to [lambda][x][y] + big-endian) on the
+    GPU: algorithmic bytes 2 C per launch (read + write), against the HBM peak."""
+    from rubix_gb300 import ops
+
+    out = ops.fits_cube_layout(cube)
+    ms = _time_steps(lambda: ops.fits_cube_layout(cube, out=out), steps, warmup, flush)
+    nbytes = 2 * cube.numel() * 4
+    peak, kind = hbm_peak()
+    return {"kernel": "rubix_fits_cube_layout", "ms": ms, "achieved_gbs": nbytes / ms / 1e6,
+            "peak_gbs": peak, "frac": nbytes / ms / 1e6 / peak, "peak_source": kind,
+            "bytes": nbytes}
+
+
 # The plain GPU path: the same algorithm written with stock torch operations (gathers,
 # searchsorted, index_add_, conv2d, conv1d) on the same GPU, materialising the
 # per-particle spectra like the reference's step functions do.
@@ -708,6 +722,7 @@ def main():
                                                   args.warmup, flush)),
                 ("plain_gpu_fwd_bwd", lambda: plain_fwd_bwd_bench(dev, args.steps, 1)),
                 ("dusty", lambda: dusty_bench(dev, w, d_in, args.steps, 3, flush)),
+                ("fits_layout", lambda: fits_bench(dev, ours_final, args.steps, 3, flush)),
                 ("ragged", lambda: ragged_bench(dev, 3, 2))):
             try:
                 extras[name] = fn()
