@@ -57,6 +57,8 @@ struct MainArgs {
   CubeCtrl* ctrl;
   const int2* bucket;
   int row_cap;
+  int staged;           // corner segments staged in shared memory by TMA (else read from L2)
+  int pool;             // entries of the row pool (and of the staging pool when staged)
   int chunk;            // particles per work item
   int lsf_k, lsf_crop;  // lsf_k = 0: no LSF epilogue
   float lsf[kMaxLsfTaps + 1];
@@ -64,21 +66,21 @@ struct MainArgs {
 };
 
 // Shared-memory carve-up of the main kernel (byte offsets, 16-byte aligned): the TMA
-// staging pool and the row pool, P = kPB * row_cap entries each, shared by the up to
-// kPBMax particles of a batch.
+// staging pool (`stage` entries; none when corners are read from L2) and the row pool
+// (`pool` entries), shared by the up to kPBMax particles of a batch.
 struct SmemLayout {
   size_t wz, bucket, stage, rows, red, rec, total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int n_wave, int row_cap) {
+__host__ __device__ inline SmemLayout smem_layout(int n_wave, int stage, int pool) {
   SmemLayout L;
   size_t o = 0;
   auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
   L.wz = o;     o = al(o + sizeof(float) * n_wave);
   L.bucket = o; o = al(o + sizeof(int2) * kBuckets);
-  L.stage = o;  o = al(o + sizeof(float4) * kPB * (size_t)row_cap);
+  L.stage = o;  o = al(o + sizeof(float4) * (size_t)stage);
   L.rows = o;   // also holds the zero-padded spectrum of the LSF epilogue
-  o = al(o + std::max(sizeof(float4) * kPB * (size_t)row_cap,
+  o = al(o + std::max(sizeof(float4) * (size_t)pool,
                       sizeof(float) * (size_t)(kMaxWaveT + 2 * kMaxLsfTaps + 8)));
   L.red = o;    o = al(o + sizeof(float) * 2 * kAccWarps * 4);
   L.rec = o;    o = al(o + sizeof(ParticleRec) * kMaxChunk);
@@ -155,6 +157,7 @@ struct RowParams {
   float4* row;
 };
 
+template <bool kStaged>
 __device__ __forceinline__ RowParams row_params(const ParticleRec& r, const MainArgs& a,
                                                 const float4* stage, float4* row) {
   RowParams q;
@@ -170,7 +173,12 @@ __device__ __forceinline__ RowParams row_params(const ParticleRec& r, const Main
   q.khi = min(ke + 1, a.n_wave - 1);
   q.n_e = ke - q.ks + 1;
   q.has_cell = r.b.x >= 0;
-  q.st = stage - q.klo;
+  // staged: the segment [klo, khi] in shared memory; else the cell's corner-table row
+  // (row 0 stands in for particles outside the grid, whose G is forced to 0)
+  if constexpr (kStaged)
+    q.st = stage - q.klo;
+  else
+    q.st = a.ct + (long long)max(r.b.x, 0) * a.n_wave;
   q.row = row;
   return q;
 }
@@ -299,17 +307,18 @@ __device__ __forceinline__ void build_step_pair2(const RowParams& q, int b0, int
 // Builds the rows of a planned batch (1..3 particles) from the staged corners: the
 // first two particles' 31-entry steps interleaved, the third's interleaved with its
 // own next step.
+template <bool kStaged>
 __device__ __forceinline__ void build_plan(const MainArgs& a, const ParticleRec* recs,
                                            const BatchPlan& bp, const float* __restrict__ s_wz,
                                            const float4* __restrict__ stage,
                                            float4* __restrict__ rows, int lane, int warp) {
-  const RowParams q0 = row_params(recs[0], a, stage, rows);
+  const RowParams q0 = row_params<kStaged>(recs[0], a, stage, rows);
   if (bp.cnt == 1) {
     for (int base = warp * 31; base < q0.n_e; base += kAccWarps * 31)
       build_step(q0, base, a.n_wave, s_wz, lane);
     return;
   }
-  const RowParams q1 = row_params(recs[1], a, stage + bp.off[1], rows + bp.off[1]);
+  const RowParams q1 = row_params<kStaged>(recs[1], a, stage + bp.off[1], rows + bp.off[1]);
   const int n_max = max(q0.n_e, q1.n_e);
   for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
     if (base < q0.n_e && base < q1.n_e && interior(q0, base) && interior(q1, base)) {
@@ -320,7 +329,7 @@ __device__ __forceinline__ void build_plan(const MainArgs& a, const ParticleRec*
     }
   }
   if (bp.cnt == 3) {
-    const RowParams q2 = row_params(recs[2], a, stage + bp.off[2], rows + bp.off[2]);
+    const RowParams q2 = row_params<kStaged>(recs[2], a, stage + bp.off[2], rows + bp.off[2]);
     for (int base = warp * 31; base < q2.n_e; base += 2 * kAccWarps * 31) {
       const int b2 = base + kAccWarps * 31;
       if (b2 < q2.n_e && interior(q2, base) && interior(q2, b2)) {
@@ -526,10 +535,10 @@ __device__ __forceinline__ void lsf_epilogue_k(const MainArgs& a,
   }
 }
 
-template <int R, bool kDust>
+template <int R, bool kDust, bool kStaged>
 __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const SmemLayout SL = smem_layout(a.n_wave, a.row_cap);
+  const SmemLayout SL = smem_layout(kStaged ? a.n_wave : 0, kStaged ? a.pool : 0, a.pool);
   float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
   int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
   float4* s_stage = reinterpret_cast<float4*>(smem + SL.stage);      // pool of P entries
@@ -541,8 +550,10 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   __shared__ int s_item, s_last, s_fail;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < a.n_wave; i += kAccThreads) s_wz[i] = a.wave_z[i];
+  if constexpr (kStaged)
+    for (int i = tid; i < a.n_wave; i += kAccThreads) s_wz[i] = a.wave_z[i];
   for (int b = tid; b < kBuckets; b += kAccThreads) s_bucket[b] = a.bucket[b];
+  const float* wzp = kStaged ? s_wz : a.wave_z;  // SSP wavelengths: shared or L1
   if (tid == 0) {
     mbar_init(&s_bar, 1);
     fence_mbar_init();
@@ -551,7 +562,8 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
 
   const int n_t = a.n_t;
   const int t0 = tid * R;
-  const int P = kPB * a.row_cap;
+  const int P = a.pool;
+  constexpr bool staged = kStaged;
   float lam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -585,7 +597,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
     for (int i = tid; i < np; i += kAccThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
     BatchPlan bp = plan_batch(s_rec, np, P);
-    if (np > 0 && tid == 0) issue_plan(a, s_rec, bp, s_stage, &s_bar);
+    if (staged && np > 0 && tid == 0) issue_plan(a, s_rec, bp, s_stage, &s_bar);
 
     // Batch at p0: wait for its staged corners, build its rows, stage the next batch,
     // evaluate, reduce T'.
@@ -593,9 +605,11 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       const int buf = step & 1;
       const int cnt = bp.cnt;
       const ParticleRec* recs = s_rec + p0;
-      if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
-      phase ^= 1u;
-      build_plan(a, recs, bp, s_wz, s_stage, s_rows, lane, warp);
+      if (staged) {
+        if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
+        phase ^= 1u;
+      }
+      build_plan<kStaged>(a, recs, bp, wzp, s_stage, s_rows, lane, warp);
       __syncthreads();  // rows ready; staging consumed
       if (s_fail) {
         if (tid == 0) {
@@ -606,7 +620,7 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       }
       const int p1 = p0 + cnt;
       const BatchPlan bn = plan_batch(s_rec + p1, np - p1, P);
-      if (p1 < np && tid == 0) issue_plan(a, s_rec + p1, bn, s_stage, &s_bar);
+      if (staged && p1 < np && tid == 0) issue_plan(a, s_rec + p1, bn, s_stage, &s_bar);
 
       float I[kPBMax][R];
       float tp[kPBMax];
@@ -748,15 +762,15 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   }
 }
 
-template <int R, bool kDust>
+template <int R, bool kDust, bool kStaged>
 int launch_main_t(const MainArgs& args, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(cube_main_kernel<R, kDust>,
+  cudaError_t e = cudaFuncSetAttribute(cube_main_kernel<R, kDust, kStaged>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess)
     return set_error(RUBIX_E_CUDA, "cudaFuncSetAttribute(cube_main_kernel): %s",
                      cudaGetErrorString(e));
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_main_kernel<R, kDust>,
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cube_main_kernel<R, kDust, kStaged>,
                                                     kAccThreads,
                                                     smem);
   if (e != cudaSuccess || per_sm < 1)
@@ -764,15 +778,18 @@ int launch_main_t(const MainArgs& args, size_t smem, cudaStream_t st) {
                      "cube_main_kernel does not fit on an SM with %zu bytes of shared memory",
                      smem);
   const int grid = sm_count() * per_sm;
-  cube_main_kernel<R, kDust><<<grid, kAccThreads, smem, st>>>(args);
+  cube_main_kernel<R, kDust, kStaged><<<grid, kAccThreads, smem, st>>>(args);
   RUBIX_LAUNCH_CHECK("cube_main_kernel");
   return RUBIX_OK;
 }
 
 template <int R>
 int launch_main(const MainArgs& args, size_t smem, cudaStream_t st) {
-  return args.dust_e2 ? launch_main_t<R, true>(args, smem, st)
-                      : launch_main_t<R, false>(args, smem, st);
+  if (args.staged)
+    return args.dust_e2 ? launch_main_t<R, true, true>(args, smem, st)
+                        : launch_main_t<R, false, true>(args, smem, st);
+  return args.dust_e2 ? launch_main_t<R, true, false>(args, smem, st)
+                      : launch_main_t<R, false, false>(args, smem, st);
 }
 
 int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metallicity,
@@ -836,10 +853,19 @@ int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
                 "%s: workspace of %zu bytes needed, %zu given", who, need, workspace_bytes);
   RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
                 "%s: workspace must be 256-byte aligned", who);
+  // Up to about 1300 SSP wavelengths two blocks with staged corners fit on an SM, up to
+  // about 3000 one.  Larger grids (to about 13 000 wavelengths) read the corners and the
+  // SSP wavelengths through L1/L2 instead of staging them, with one or two rows in the
+  // pool.
   const int row_cap = n_wave + 2;
-  const SmemLayout SL = smem_layout(n_wave, row_cap);
-  // Up to about 1300 SSP wavelengths two blocks fit on an SM; larger grids run one.
-  RUBIX_REQUIRE(SL.total <= 227 * 1024, RUBIX_E_UNSUPPORTED,
+  constexpr size_t kSmemMax = 227 * 1024;
+  int staged = 1, pool = kPB * row_cap;
+  if (smem_layout(n_wave, pool, pool).total > kSmemMax) {
+    staged = 0;
+    if (smem_layout(0, 0, pool).total > kSmemMax) pool = row_cap;
+  }
+  const SmemLayout SL = smem_layout(staged ? n_wave : 0, staged ? pool : 0, pool);
+  RUBIX_REQUIRE(SL.total <= kSmemMax, RUBIX_E_UNSUPPORTED,
                 "%s: SSP grid of %d wavelengths needs %zu bytes of shared memory "
                 "(limit 232448)",
                 who, n_wave, SL.total);
@@ -875,6 +901,8 @@ int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
   args.ctrl = L.ctrl;
   args.bucket = L.bucket;
   args.row_cap = row_cap;
+  args.staged = staged;
+  args.pool = pool;
   args.chunk = tune.chunk;
   args.lsf_k = n_lsf_taps;
   args.lsf_crop = lsf_crop;

@@ -51,6 +51,7 @@ struct AdjArgs {
   CubeCtrl* ctrl;
   const int2* bucket;
   int row_cap;
+  int staged;  // corner segments and SSP wavelengths in shared memory (else via L1/L2)
   int chunk;
   const float* dust_e2;  // per telescope wavelength: -0.4 log2(10) A(lambda)/A(V)
 };
@@ -59,14 +60,15 @@ struct AdjSmem {
   size_t wz, bucket, grid, stage, row_a, row_b, red, rec, total;
 };
 
-__host__ __device__ inline AdjSmem adj_smem_layout(int n_wave, int n_grid, int row_cap) {
+__host__ __device__ inline AdjSmem adj_smem_layout(int n_wave, int n_grid, int row_cap,
+                                                   bool staged) {
   AdjSmem L;
   size_t o = 0;
   auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
-  L.wz = o;     o = al(o + sizeof(float) * n_wave);
+  L.wz = o;     o = al(o + sizeof(float) * (staged ? n_wave : 0));
   L.bucket = o; o = al(o + sizeof(int2) * kBuckets);
   L.grid = o;   o = al(o + sizeof(float) * n_grid);
-  L.stage = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
+  L.stage = o;  o = al(o + sizeof(float4) * (staged ? (size_t)row_cap : 0));
   L.row_a = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
   L.row_b = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
   L.red = o;    o = al(o + sizeof(float) * 2 * kAdjWarps * kAdjSums);
@@ -119,7 +121,8 @@ __device__ __forceinline__ void adj_build(const AdjArgs& a, const ParticleRec& r
     a0 = (1.f - tz) * iaw;  // GA = a0 (F01 - F00) + a1 (F11 - F10)
     a1 = tz * iaw;
   }
-  const float4* st = stage - klo;
+  // staged: the segment [klo, khi] in shared memory; else the cell's corner-table row
+  const float4* st = a.staged ? stage - klo : a.ct + (long long)max(cell, 0) * nW;
   for (int base = warp * 31; base < n_e; base += kAdjWarps * 31) {
     const int e = base + lane;
     const int k = ks + e;
@@ -256,7 +259,7 @@ __device__ __forceinline__ float warp_reduce8(const float (&v)[8], int lane) {
 template <int R, bool kDust>
 __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const AdjSmem SL = adj_smem_layout(a.n_wave, a.nZ + a.nA, a.row_cap);
+  const AdjSmem SL = adj_smem_layout(a.n_wave, a.nZ + a.nA, a.row_cap, a.staged != 0);
   float* s_wz = reinterpret_cast<float*>(smem + SL.wz);
   int2* s_bucket = reinterpret_cast<int2*>(smem + SL.bucket);
   float* s_grid = reinterpret_cast<float*>(smem + SL.grid);
@@ -269,7 +272,10 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
   __shared__ int s_item, s_fail;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < a.n_wave; i += kAdjThreads) s_wz[i] = a.wave_z[i];
+  if (a.staged)
+    for (int i = tid; i < a.n_wave; i += kAdjThreads) s_wz[i] = a.wave_z[i];
+  const float* wzp = a.staged ? s_wz : a.wave_z;  // SSP wavelengths: shared or L1
+  const bool staged = a.staged != 0;
   for (int b = tid; b < kBuckets; b += kAdjThreads) s_bucket[b] = a.bucket[b];
   for (int i = tid; i < a.nZ; i += kAdjThreads) s_grid[i] = a.zg[i];
   for (int i = tid; i < a.nA; i += kAdjThreads) s_grid[a.nZ + i] = a.ag[i];
@@ -310,14 +316,16 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
     for (int r = 0; r < R; ++r) h[r] = (t0 + r < n_t) ? adj[t0 + r] : 0.f;
     for (int i = tid; i < np; i += kAdjThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
-    if (np > 0 && tid == 0) adj_issue(a, s_rec[0], s_stage, &s_bar);
+    if (staged && np > 0 && tid == 0) adj_issue(a, s_rec[0], s_stage, &s_bar);
 
     for (int p = 0; p < np; ++p, ++step) {
       const int buf = step & 1;
       const ParticleRec& rec = s_rec[p];
-      if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
-      phase ^= 1u;
-      adj_build(a, rec, s_wz, s_grid, s_stage, s_ra, s_rb, lane, warp);
+      if (staged) {
+        if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
+        phase ^= 1u;
+      }
+      adj_build(a, rec, wzp, s_grid, s_stage, s_ra, s_rb, lane, warp);
       __syncthreads();  // rows ready; staging consumed
       if (s_fail) {
         if (tid == 0) {
@@ -326,7 +334,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
         }
         return;
       }
-      if (p + 1 < np && tid == 0) adj_issue(a, s_rec[p + 1], s_stage, &s_bar);
+      if (staged && p + 1 < np && tid == 0) adj_issue(a, s_rec[p + 1], s_stage, &s_bar);
       const int4 rb = rec.b;
       const int ks = rb.y, ke = rb.z & ~kGenericFlag;
       float sums[kAdjSums];
@@ -454,8 +462,11 @@ int cube_bwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
                 "%s: workspace of %zu bytes needed, %zu given", who, need, workspace_bytes);
   RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
                 "%s: workspace must be 256-byte aligned", who);
+  // Grids too large for the staged layout (about 4000 SSP wavelengths) read the corners
+  // and the SSP wavelengths through L1/L2 (to about 6500 wavelengths).
   const int row_cap = n_wave + 2;
-  const AdjSmem SL = adj_smem_layout(n_wave, n_met + n_age, row_cap);
+  const bool staged = adj_smem_layout(n_wave, n_met + n_age, row_cap, true).total <= 227 * 1024;
+  const AdjSmem SL = adj_smem_layout(n_wave, n_met + n_age, row_cap, staged);
   RUBIX_REQUIRE(SL.total <= 227 * 1024, RUBIX_E_UNSUPPORTED,
                 "%s: SSP grid of %d wavelengths needs %zu bytes of shared memory "
                 "(limit 232448)",
@@ -495,6 +506,7 @@ int cube_bwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
   args.ctrl = L.ctrl;
   args.bucket = L.bucket;
   args.row_cap = row_cap;
+  args.staged = staged ? 1 : 0;
   args.chunk = tune.chunk;
   args.dust_e2 = dust_e2;
   const int need_r = (n_wave_t + kAdjThreads - 1) / kAdjThreads;
