@@ -54,6 +54,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the fwd+bwd, plain-GPU-path and ragged-batch measurements")
+    ap.add_argument("--dust", type=int, default=0, metavar="N_GAS",
+                    help="measure the dusty step (calc_dusty_ifu) with N_GAS gas cells as "
+                         "the main line (device time; no e2e)")
     return ap.parse_args()
 
 
@@ -586,8 +589,15 @@ def main():
     p = w.particles
     N, L = p.n, int(w.wave_t.size)
     S2 = w.sbin * w.sbin
-    rnd = IFURenderer.from_workload(w, device=dev)
+    dusty = args.dust > 0
+    rnd = IFURenderer.from_workload(w, device=dev, dust={"extinction_model": "Cardelli89",
+                                                         "Rv": 3.1} if dusty else None)
     d_in = [torch.from_numpy(a).to(dev) for a in (p.coords, p.velocity, p.mass, p.metallicity, p.age)]
+    gas = None
+    if dusty:
+        g = synth.make_gas(args.dust, seed=rdist.rank_seed(2, rank))
+        gas = tuple(torch.from_numpy(a).to(dev) for a in (g.coords, g.mass, g.metals))
+        args.no_e2e = True
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
     def barrier():
@@ -597,9 +607,11 @@ def main():
     def step_device(ev=None):
         idx, mask = rnd.assign(d_in[0])
         perm, offs = rnd.sort(idx, mask)
+        av = rnd.dust_av(d_in[0], idx, *gas) if dusty else None
         if ev is not None:
             ev[0].record()
-        cube = rnd.accumulate(d_in[2], d_in[3], d_in[4], d_in[1], perm, offs, with_lsf=True)
+        cube = rnd.accumulate(d_in[2], d_in[3], d_in[4], d_in[1], perm, offs, with_lsf=True,
+                              dust_av=av)
         if ev is not None:
             ev[1].record()
         return rnd.noise_(rnd.psf(cube))
@@ -737,13 +749,19 @@ def main():
                 extras["fwd_bwd"]["value"] / extras["plain_gpu_fwd_bwd"]["value"])
 
     if rank == 0:
+        cfg = workload_config(w)
+        if dusty:
+            cfg["path"] = cfg["path"].replace("mask+assign+sort", "mask+assign+sort -> A_V "
+                                              f"of every star from {args.dust} gas cells")
+            cfg["dust"] = "Cardelli89, R_V 3.1, broken power-law dust-to-gas ratio (X_CO = Z)"
         line = {
-            "metric": "particles*lambda/s, particle->IFU datacube forward",
+            "metric": "particles*lambda/s, particle->IFU datacube forward"
+                      + (" with dust extinction" if dusty else ""),
             "value": value, "unit": "particle*lambda/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(step_ms),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded exponential disk; synthetic SSP grid)",
-            "config": workload_config(w), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches, "clocks": clocks, "wall_s_timed": wall,
         }
         line.update(extras)

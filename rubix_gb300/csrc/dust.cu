@@ -104,9 +104,18 @@ __global__ void dust_segoff_kernel(const unsigned* __restrict__ keys, long long 
   }
 }
 
+// The cells' extinction in P order (so that the segmented sums read contiguously).
+__global__ void dust_gather_kernel(const float* __restrict__ ext, const int* __restrict__ perm,
+                                   long long n, float* __restrict__ ext_p) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x)
+    ext_p[j] = ext[perm[j]];
+}
+
 // Inclusive cumulative sum of the cells' extinction within each segment, in P order:
-// one warp per segment, 32 cells per step with a running carry.
-__global__ void dust_cumsum_kernel(const float* __restrict__ ext, const int* __restrict__ perm,
+// one warp per segment, 4 x 32 cells loaded ahead, then scanned 32 at a time with a
+// running carry.
+__global__ void dust_cumsum_kernel(const float* __restrict__ ext_p,
                                    const int* __restrict__ seg_off, int nseg,
                                    float* __restrict__ cum) {
   const int lane = threadIdx.x & 31;
@@ -114,17 +123,26 @@ __global__ void dust_cumsum_kernel(const float* __restrict__ ext, const int* __r
   for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nseg; s += warps) {
     const int b = seg_off[s], e = seg_off[s + 1];
     float carry = 0.f;
-    for (int base = b; base < e; base += 32) {
-      const int j = base + lane;
-      float v = j < e ? ext[perm[j]] : 0.f;
+    for (int base = b; base < e; base += 128) {
+      float v[4];
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const float y = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v = __fadd_rn(v, y);
+      for (int q = 0; q < 4; ++q) {
+        const int j = base + 32 * q + lane;
+        v[q] = j < e ? ext_p[j] : 0.f;
       }
-      v = __fadd_rn(v, carry);
-      if (j < e) cum[j] = v;
-      carry = __shfl_sync(0xffffffffu, v, 31);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float x = v[q];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x = __fadd_rn(x, y);
+        }
+        x = __fadd_rn(x, carry);
+        const int j = base + 32 * q + lane;
+        if (j < e) cum[j] = x;
+        carry = __shfl_sync(0xffffffffu, x, 31);
+      }
     }
   }
 }
@@ -451,8 +469,10 @@ extern "C" int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const 
     const int* vp = w ? vo : vz;
     RUBIX_CUDA_TRY(cudaMemcpyAsync(L.perm, vp, sizeof(int) * ng, cudaMemcpyDeviceToDevice, st));
     dust_segoff_kernel<<<grid_for(ng + 1, 256), 256, 0, st>>>(kp, ng, n_segments, L.seg_off);
+    // L.nz holds the P-ordered extinction until the node pass overwrites it
+    dust_gather_kernel<<<G, 256, 0, st>>>(gas_ext, L.perm, ng, L.nz);
     dust_cumsum_kernel<<<grid_for((long long)n_segments * 32, 256), 256, 0, st>>>(
-        gas_ext, L.perm, L.seg_off, n_segments, L.cum);
+        L.nz, L.seg_off, n_segments, L.cum);
     // Q order: only differs from P order when assignments reach past the last spaxel.
     const int* qpos = nullptr;
     if (pa_limit > n_segments) {
@@ -491,8 +511,10 @@ extern "C" int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const 
     v.rid = L.rid;
     v.run_start = L.run_start;
   }
-  dust_star_av_kernel<<<grid_for(n_stars, 256), 256, 0, st>>>(v, star_coords, star_stride,
-                                                               star_pa, n_stars, av_out);
+  // one star per thread: the binary searches are latency-bound, so no grid cap
+  const long long star_blocks = (n_stars + 255) / 256;
+  dust_star_av_kernel<<<(unsigned)std::min<long long>(star_blocks, 1LL << 30), 256, 0, st>>>(
+      v, star_coords, star_stride, star_pa, n_stars, av_out);
   RUBIX_LAUNCH_CHECK("dust_star_av_kernel");
   return RUBIX_OK;
 }

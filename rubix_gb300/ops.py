@@ -509,7 +509,7 @@ def dust_av(gas_coords, gas_pa, gas_ext, star_coords, star_pa, n_segments: int,
         if ng > 0:
             # z sort, assignment sort, G sort (4 + P + 4 radix passes of 3 launches each)
             # plus the key, offset, cumulative-sum, node, run and scan passes
-            k += 35 + 3 * _key_passes(int(pa_limit) - 1)
+            k += 36 + 3 * _key_passes(int(pa_limit) - 1)
             if pa_limit > n_segments:
                 k += 14 + 3 * _key_passes(int(n_segments) - 1)
         _count(k)
