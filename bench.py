@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the fwd+bwd, plain-GPU-path and ragged-batch measurements")
+    ap.add_argument("--ssp-wave", type=int, default=None, metavar="N",
+                    help="synthetic SSP grid with N wavelengths (e.g. 5994, FSPS-sized)")
     ap.add_argument("--dust", type=int, default=0, metavar="N_GAS",
                     help="measure the dusty step (calc_dusty_ifu) with N_GAS gas cells as "
                          "the main line (device time; no e2e)")
@@ -585,7 +587,8 @@ def main():
     _build.build()
     # every rank renders its own galaxy (independent seeds): weak scaling, no exchange
     w = synth.make_workload(args.workload, n=args.particles, edge_cases=False,
-                            seed=rdist.rank_seed(synth.WORKLOADS[args.workload]["seed"], rank))
+                            seed=rdist.rank_seed(synth.WORKLOADS[args.workload]["seed"], rank),
+                            n_wave_ssp=args.ssp_wave)
     p = w.particles
     N, L = p.n, int(w.wave_t.size)
     S2 = w.sbin * w.sbin

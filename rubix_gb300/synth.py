@@ -209,13 +209,17 @@ class Workload:
 
 
 def make_workload(name: str, n: int | None = None, edge_cases: bool = True,
-                  n_wave_t: int | None = None, seed: int | None = None) -> Workload:
+                  n_wave_t: int | None = None, seed: int | None = None,
+                  n_wave_ssp: int | None = None) -> Workload:
     """Build a named workload; ``n`` overrides the particle count, ``n_wave_t`` truncates
-    the telescope grid (for fast CPU checks), ``seed`` the particle seed."""
+    the telescope grid (for fast CPU checks), ``seed`` the particle seed, ``n_wave_ssp``
+    the number of SSP wavelengths."""
     cfg = dict(WORKLOADS[name])
     if seed is not None:
         cfg["seed"] = seed
     n_age, n_met, n_wave = cfg["ssp"]
+    if n_wave_ssp is not None:
+        n_wave = int(n_wave_ssp)
     ssp = make_ssp(n_age, n_met, n_wave, seed=WORKLOADS[name]["seed"])
     sbin = int(np.floor(cfg["fov"] / SPATIAL_RES))
     edges, _ = tel.spatial_bin_edges(cfg["fov"], sbin, DIST_Z)
