@@ -70,6 +70,35 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def fp32_peak_tflops(dev, reps=5):
+    """FP32 FMA rate of this GPU from the library's FMA-chain probe (best of reps)."""
+    import torch
+
+    from rubix_gb300 import ops
+
+    best = 0.0
+    for i in range(reps + 2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        n_fma, _ = ops.fma_probe(dev)
+        e1.record()
+        torch.cuda.synchronize()
+        if i >= 2:
+            best = max(best, 2.0 * n_fma / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def flops_per_particle_lambda(w):
+    """Algorithmic FP32 operations of kernel (b) per (particle, telescope wavelength):
+    the evaluation does 7 (x - lambda'_k, the interpolation FMA, T' FMA, accumulation
+    FMA) plus the bin width shared by a batch (about 0.4); the row build does 11 per SSP
+    entry (four-corner mix 7, lambda' 1, slope 3) over the n_e entries that span the
+    telescope range, spread over the L wavelengths."""
+    t0, t1 = float(w.wave_t[0]), float(w.wave_t[-1])
+    n_e = int(np.count_nonzero((w.wave_z >= t0) & (w.wave_z <= t1))) + 2
+    return 7.4 + 11.0 * n_e / float(w.wave_t.size)
+
+
 def traffic_per_launch(n_particles):
     """DRAM bytes per rubix_cube_fwd launch from the committed ncu summary, scaled to
     the particle count of this run (the summary states the captured count)."""
@@ -710,12 +739,20 @@ def main():
     cube_avg_s = statistics.mean(cube_ms) * 1e-3
     achieved = alg_bytes / cube_avg_s / 1e9
     traffic = traffic_per_launch(N)
+    fpl = flops_per_particle_lambda(w)
+    fp32_peak = fp32_peak_tflops(dev)
+    fp32_achieved = fpl * N * L / cube_avg_s / 1e12
+    compute = {"fp32_peak_tflops": fp32_peak, "peak_source": "measured FMA-chain probe "
+               "(rubix_fma_probe)", "achieved_tflops": fp32_achieved,
+               "frac": fp32_achieved / fp32_peak if fp32_peak else None,
+               "flops_per_particle_lambda": fpl}
     roofline = {"kernel": "rubix_cube_fwd (fused lookup/mass/Doppler/resample/accumulate)",
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                 "traffic": traffic, "algorithmic_bytes": alg_bytes,
                 "ms_per_launch": statistics.mean(cube_ms),
-                "share_of_step": statistics.mean(cube_ms) / statistics.mean(step_ms)}
+                "share_of_step": statistics.mean(cube_ms) / statistics.mean(step_ms),
+                "fp32": compute}
 
     # ---------------- CPU baseline (rank 0, N=1): oracle port, one core, bounded sample
     cpu = None

@@ -243,6 +243,17 @@ RUBIX_API int rubix_fits_cube_layout(const float* cube, int32_t A, int32_t B, in
                                      int64_t spaxel_stride, void* out, void* stream);
 
 /*
+ * No counterpart in rubix (a measurement aid).
+ *
+ * rubix_fma_probe_blocks() blocks of 256 threads each run iters * 128 dependent-chain
+ * FP32 FMAs (8 chains per thread) and store one float per thread into out
+ * (rubix_fma_probe_blocks() * 256 floats): timing a launch gives the FP32 FMA rate
+ * against which the compute roofline of the kernels is stated.
+ */
+RUBIX_API int rubix_fma_probe_blocks(void);
+RUBIX_API int rubix_fma_probe(float* out, int32_t iters, void* stream);
+
+/*
  * No counterpart in rubix (rubix has no C interface; JAX allocates its buffers).
  *
  * rubix_cube_fwd without the workspace argument, for callers that cannot allocate
