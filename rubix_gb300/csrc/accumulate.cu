@@ -17,9 +17,10 @@
 //   * A batch is 1-3 particles packed by their bracket lengths into staging and row
 //     pools of kPB * (nW + 2) entries.  One thread issues a 1-D TMA bulk copy of each
 //     particle's corner-table segment (its bracket range only) into the staging pool; it
-//     completes on an mbarrier while the block evaluates the previous batch.  The block
-//     then builds per particle the row of entries (lambda'_k, slope_k, G_k,
-//     lambda'_{k+1}) of the mixed template G = sum_c w_c F_c; the in-range flux sum T
+//     completes on an mbarrier while the block evaluates the previous batch.  The
+//     warps, split evenly over the batch's particles, then build per particle the row of
+//     entries (lambda'_k, slope_k, G_k, lambda'_{k+1}) of the mixed template
+//     G = sum_c w_c F_c; the in-range flux sum T
 //     (rubix/spectra/ifu.py:241-245) comes from the gather (prefix sums).
 //   * Evaluation: each thread finds the exact bracket of its first wavelength (bucket
 //     table + exact comparisons on lambda') and walks forward over its R wavelengths;
@@ -234,41 +235,10 @@ __device__ __forceinline__ void build_step(const RowParams& q, int base, int nW,
   }
 }
 
-// Interior build steps of two particles at the same base, interleaved: both particles'
-// corner loads, mixes, shuffles and slopes are independent, so their latencies overlap.
+// A build step is interior when every lane, neighbour included, is an SSP wavelength of
+// the particle's staged range.
 __device__ __forceinline__ bool interior(const RowParams& q, int base) {
   return q.ks + base >= 0 && q.ks + base + 31 <= q.khi;
-}
-
-__device__ __forceinline__ void build_step_pair(const RowParams& q0, const RowParams& q1,
-                                                int base, const float* __restrict__ s_wz,
-                                                int lane) {
-  const int e = base + lane;
-  const int k0 = q0.ks + e, k1 = q1.ks + e;
-  const float4 c0 = q0.st[k0];
-  const float4 c1 = q1.st[k1];
-  const float z0 = s_wz[k0], z1 = s_wz[k1];
-  float G0 = q0.w00 * c0.x, G1 = q1.w00 * c1.x;
-  G0 = fmaf(q0.w10, c0.y, G0);
-  G1 = fmaf(q1.w10, c1.y, G1);
-  G0 = fmaf(q0.w01, c0.z, G0);
-  G1 = fmaf(q1.w01, c1.z, G1);
-  G0 = fmaf(q0.w11, c0.w, G0);
-  G1 = fmaf(q1.w11, c1.w, G1);
-  if (!q0.has_cell) G0 = 0.f;
-  if (!q1.has_cell) G1 = 0.f;
-  const float lp0 = __fmul_rn(z0, q0.alpha), lp1 = __fmul_rn(z1, q1.alpha);
-  const float lpn0 = __shfl_down_sync(0xffffffffu, lp0, 1);
-  const float lpn1 = __shfl_down_sync(0xffffffffu, lp1, 1);
-  const float Gn0 = __shfl_down_sync(0xffffffffu, G0, 1);
-  const float Gn1 = __shfl_down_sync(0xffffffffu, G1, 1);
-  if (lane < 31) {
-    const float dl0 = lpn0 - lp0, dl1 = lpn1 - lp1;
-    const float sl0 = dl0 > 0.f ? __fdividef(Gn0 - G0, dl0) : 0.f;
-    const float sl1 = dl1 > 0.f ? __fdividef(Gn1 - G1, dl1) : 0.f;
-    q0.row[e] = make_float4(lp0, sl0, G0, lpn0);
-    q1.row[e] = make_float4(lp1, sl1, G1, lpn1);
-  }
 }
 
 // Two interior steps of one particle at two bases, interleaved.
@@ -304,40 +274,29 @@ __device__ __forceinline__ void build_step_pair2(const RowParams& q, int b0, int
   }
 }
 
-// Builds the rows of a planned batch (1..3 particles) from the staged corners: the
-// first two particles' 31-entry steps interleaved, the third's interleaved with its
-// own next step.
+// Builds the rows of a planned batch (1..3 particles) from the staged corners.  The
+// 12 warps are split evenly over the batch's particles (12, 6 or 4 warps each), so each
+// warp derives one particle's row parameters; a warp interleaves two 31-entry steps of
+// its particle for instruction-level parallelism.
 template <bool kStaged>
 __device__ __forceinline__ void build_plan(const MainArgs& a, const ParticleRec* recs,
                                            const BatchPlan& bp, const float* __restrict__ s_wz,
                                            const float4* __restrict__ stage,
                                            float4* __restrict__ rows, int lane, int warp) {
-  const RowParams q0 = row_params<kStaged>(recs[0], a, stage, rows);
-  if (bp.cnt == 1) {
-    for (int base = warp * 31; base < q0.n_e; base += kAccWarps * 31)
-      build_step(q0, base, a.n_wave, s_wz, lane);
-    return;
-  }
-  const RowParams q1 = row_params<kStaged>(recs[1], a, stage + bp.off[1], rows + bp.off[1]);
-  const int n_max = max(q0.n_e, q1.n_e);
-  for (int base = warp * 31; base < n_max; base += kAccWarps * 31) {
-    if (base < q0.n_e && base < q1.n_e && interior(q0, base) && interior(q1, base)) {
-      build_step_pair(q0, q1, base, s_wz, lane);
+  const int cnt = bp.cnt;
+  const int wpp = kAccWarps / cnt;  // kAccWarps is divisible by 1, 2 and 3
+  const int p = warp / wpp;
+  const int wl = warp - p * wpp;
+  const int off = p == 0 ? 0 : (p == 1 ? bp.off[1] : bp.off[2]);
+  const RowParams q = row_params<kStaged>(recs[p], a, stage + off, rows + off);
+  const int stride = wpp * 31;
+  for (int base = wl * 31; base < q.n_e; base += 2 * stride) {
+    const int b2 = base + stride;
+    if (b2 < q.n_e && interior(q, base) && interior(q, b2)) {
+      build_step_pair2(q, base, b2, s_wz, lane);
     } else {
-      if (base < q0.n_e) build_step(q0, base, a.n_wave, s_wz, lane);
-      if (base < q1.n_e) build_step(q1, base, a.n_wave, s_wz, lane);
-    }
-  }
-  if (bp.cnt == 3) {
-    const RowParams q2 = row_params<kStaged>(recs[2], a, stage + bp.off[2], rows + bp.off[2]);
-    for (int base = warp * 31; base < q2.n_e; base += 2 * kAccWarps * 31) {
-      const int b2 = base + kAccWarps * 31;
-      if (b2 < q2.n_e && interior(q2, base) && interior(q2, b2)) {
-        build_step_pair2(q2, base, b2, s_wz, lane);
-      } else {
-        build_step(q2, base, a.n_wave, s_wz, lane);
-        if (b2 < q2.n_e) build_step(q2, b2, a.n_wave, s_wz, lane);
-      }
+      build_step(q, base, a.n_wave, s_wz, lane);
+      if (b2 < q.n_e) build_step(q, b2, a.n_wave, s_wz, lane);
     }
   }
 }
