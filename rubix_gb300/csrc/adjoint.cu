@@ -90,37 +90,42 @@ __device__ __forceinline__ void adj_issue(const AdjArgs& a, const ParticleRec& r
   if (b.x >= 0) bulk_copy_g2s(stage, a.ct + (long long)b.x * a.n_wave + klo, bytes, bar);
 }
 
+// The particle's mixing weights: G = w00 F00 + w10 F10 + w01 F01 + w11 F11 and the
+// derivative weights GZ = z0 (F10 - F00) + z1 (F11 - F01), GA = a0 (F01 - F00) +
+// a1 (F11 - F10); zeros outside the grid.  One thread computes them per particle.
+__device__ __forceinline__ void adj_weights(const AdjArgs& a, const ParticleRec& r,
+                                            const float* __restrict__ s_grid, float4& w,
+                                            float4& d) {
+  w = make_float4(0.f, 0.f, 0.f, 0.f);
+  d = w;
+  const int cell = r.b.x;
+  if (cell < 0) return;
+  const float tz = r.a.w, ta = __int_as_float(r.b.w);
+  const int iz = cell / (a.nA - 1), ia = cell - iz * (a.nA - 1);
+  const float dz = s_grid[iz + 1] - s_grid[iz];
+  const float da = s_grid[a.nZ + ia + 1] - s_grid[a.nZ + ia];
+  const float izw = dz == 0.f ? 0.f : 1.f / dz, iaw = da == 0.f ? 0.f : 1.f / da;
+  w = make_float4((1.f - tz) * (1.f - ta), tz * (1.f - ta), (1.f - tz) * ta, tz * ta);
+  d = make_float4((1.f - ta) * izw, ta * izw, (1.f - tz) * iaw, tz * iaw);
+}
+
 // Row entry e (SSP index k = kstart + e): row_a = (lambda'_k, slope, G_k, lambda'_{k+1}),
 // row_b = (GZ_k, slopeZ, GA_k, slopeA) with GZ = dG/dZ, GA = dG/dage; sentinels as in
 // the forward rows (k = -1: lambda' = -FLT_MAX, value G_0, slope 0; k >= nW-1: slope 0).
 __device__ __forceinline__ void adj_build(const AdjArgs& a, const ParticleRec& r,
-                                          const float* __restrict__ s_wz,
-                                          const float* __restrict__ s_grid,
+                                          const float* __restrict__ s_wz, float4 wt, float4 dw,
                                           const float4* __restrict__ stage,
                                           float4* __restrict__ row_a, float4* __restrict__ row_b,
                                           int lane, int warp) {
   const int nW = a.n_wave;
-  const float tz = r.a.w, ta = __int_as_float(r.b.w), alpha = r.a.y;
+  const float alpha = r.a.y;
   const int ks = r.b.y, ke = r.b.z & ~kGenericFlag;
   const int klo = max(ks, 0), khi = min(ke + 1, nW - 1);
   const int n_e = ke - ks + 1;
   const int cell = r.b.x;
   const bool has_cell = cell >= 0;
-  float w00 = 0.f, w10 = 0.f, w01 = 0.f, w11 = 0.f, z0 = 0.f, z1 = 0.f, a0 = 0.f, a1 = 0.f;
-  if (has_cell) {
-    const int iz = cell / (a.nA - 1), ia = cell - iz * (a.nA - 1);
-    const float dz = s_grid[iz + 1] - s_grid[iz];
-    const float da = s_grid[a.nZ + ia + 1] - s_grid[a.nZ + ia];
-    const float izw = dz == 0.f ? 0.f : 1.f / dz, iaw = da == 0.f ? 0.f : 1.f / da;
-    w00 = (1.f - tz) * (1.f - ta);
-    w10 = tz * (1.f - ta);
-    w01 = (1.f - tz) * ta;
-    w11 = tz * ta;
-    z0 = (1.f - ta) * izw;  // GZ = z0 (F10 - F00) + z1 (F11 - F01)
-    z1 = ta * izw;
-    a0 = (1.f - tz) * iaw;  // GA = a0 (F01 - F00) + a1 (F11 - F10)
-    a1 = tz * iaw;
-  }
+  const float w00 = wt.x, w10 = wt.y, w01 = wt.z, w11 = wt.w;
+  const float z0 = dw.x, z1 = dw.y, a0 = dw.z, a1 = dw.w;
   // staged: the segment [klo, khi] in shared memory; else the cell's corner-table row
   const float4* st = a.staged ? stage - klo : a.ct + (long long)max(cell, 0) * nW;
   for (int base = warp * 31; base < n_e; base += kAdjWarps * 31) {
@@ -270,6 +275,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
   ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);
   __shared__ uint64_t s_bar;
   __shared__ int s_item, s_fail;
+  __shared__ float4 s_wt[2][2];  // mixing / derivative weights of the current, next particle
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (a.staged)
@@ -316,7 +322,11 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
     for (int r = 0; r < R; ++r) h[r] = (t0 + r < n_t) ? adj[t0 + r] : 0.f;
     for (int i = tid; i < np; i += kAdjThreads) s_rec[i] = a.rec[jb + i];
     __syncthreads();
-    if (staged && np > 0 && tid == 0) adj_issue(a, s_rec[0], s_stage, &s_bar);
+    if (np > 0 && tid == 0) {
+      if (staged) adj_issue(a, s_rec[0], s_stage, &s_bar);
+      adj_weights(a, s_rec[0], s_grid, s_wt[step & 1][0], s_wt[step & 1][1]);
+    }
+    __syncthreads();  // weights of the item's first particle visible
 
     for (int p = 0; p < np; ++p, ++step) {
       const int buf = step & 1;
@@ -325,7 +335,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
         if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
         phase ^= 1u;
       }
-      adj_build(a, rec, wzp, s_grid, s_stage, s_ra, s_rb, lane, warp);
+      adj_build(a, rec, wzp, s_wt[buf][0], s_wt[buf][1], s_stage, s_ra, s_rb, lane, warp);
       __syncthreads();  // rows ready; staging consumed
       if (s_fail) {
         if (tid == 0) {
@@ -334,7 +344,12 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
         }
         return;
       }
-      if (staged && p + 1 < np && tid == 0) adj_issue(a, s_rec[p + 1], s_stage, &s_bar);
+      if (p + 1 < np && tid == 0) {
+        // the next particle: its corner segment by TMA and its weights, read after the
+        // reduction barrier below
+        if (staged) adj_issue(a, s_rec[p + 1], s_stage, &s_bar);
+        adj_weights(a, s_rec[p + 1], s_grid, s_wt[buf ^ 1][0], s_wt[buf ^ 1][1]);
+      }
       const int4 rb = rec.b;
       const int ks = rb.y, ke = rb.z & ~kGenericFlag;
       float sums[kAdjSums];
