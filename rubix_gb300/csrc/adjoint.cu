@@ -27,6 +27,7 @@ namespace {
 
 constexpr int kAdjThreads = 384;  // 2 blocks of 12 warps per SM
 constexpr int kAdjWarps = kAdjThreads / 32;
+static_assert(kAdjWarps == 12, "the partial-sum finalize reads warps w, w + 4, w + 8");
 constexpr int kAdjSums = 8;
 
 struct AdjArgs {
@@ -367,9 +368,14 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
       }
       __syncthreads();  // partial sums visible; rows free for the next particle
       if (warp == 0) {
-        float tot = 0.f;
-        if (lane < kAdjSums)
-          for (int w = 0; w < kAdjWarps; ++w) tot += s_red[(buf * kAdjWarps + w) * kAdjSums + lane];
+        // lane l: value l & 7 over warps (l >> 3), (l >> 3) + 4, (l >> 3) + 8 (independent
+        // loads), then over the four lane groups; fixed order, so deterministic
+        const float* red = s_red + buf * kAdjWarps * kAdjSums;
+        const int vi = lane & 7, wg = lane >> 3;
+        float tot = red[wg * kAdjSums + vi] + red[(wg + 4) * kAdjSums + vi];
+        tot += red[(wg + 8) * kAdjSums + vi];
+        tot += __shfl_xor_sync(0xffffffffu, tot, 8);
+        tot += __shfl_xor_sync(0xffffffffu, tot, 16);
         const float gamma = __shfl_sync(0xffffffffu, tot, 0);
         const float Tp = __shfl_sync(0xffffffffu, tot, 1);
         const float HZ = __shfl_sync(0xffffffffu, tot, 2);
