@@ -60,6 +60,20 @@ def test_abi_version_and_workspace_queries(rubix_lib):
                                         None, None, None, 3, 2, None, None, 22500,
                                         1_000_000_000, None, 0, 0, None, 3721, None), -3,
      "static array"),
+    (lambda h: h.rubix_cube_fwd_dust(None, None, None, None, 6, 221, 1221, None, 3721, None,
+                                     None, None, None, 3, 2, None, None, None, None, 22500, 10,
+                                     None, 0, 0, None, 3721, None, 0, None), -1,
+     "null A_V or extinction exponent"),
+    (lambda h: h.rubix_dust_av(None, 3, None, None, 10, None, 3, None, 10, 0, 4, None, None, 0,
+                               None), -2, "n_segments"),
+    (lambda h: h.rubix_dust_av(None, 3, None, None, 10, None, 3, None, 10, 25, 16, None, None,
+                               0, None), -2, "n_segments <= pa_limit"),
+    (lambda h: h.rubix_dust_gas_extinction(None, None, 5, 0, 7, 10, None, 1, 1.0, 1.0, None,
+                                           None), -1, "H/O columns"),
+    (lambda h: h.rubix_fits_cube_layout(None, 4, 70000, 8, 8, None, None), -2,
+     "65535 columns"),
+    (lambda h: h.rubix_fits_cube_layout(None, 4, 4, 8, 4, None, None), -2, "spaxel_stride"),
+    (lambda h: h.rubix_fma_probe(None, 10, None), -1, "bad arguments"),
 ])
 def test_host_side_validation(rubix_lib, call, code, msg):
     rc = call(rubix_lib)

@@ -131,3 +131,16 @@ def test_capi_rejects_bad_arguments():
         ops.psf_forward(torch.zeros(4, 4, 8, device="cuda"), np.ones(65))
     with pytest.raises(ValueError):  # CPU tensors never reach the library
         ops.psf_forward(torch.zeros(4, 4, 8), np.ones(3))
+
+
+def test_fma_probe_runs():
+    """The FP32 rate probe launches, writes one finite value per thread and reports its
+    FMA count."""
+    import torch
+
+    from rubix_gb300 import ops
+
+    n_fma, out = ops.fma_probe("cuda", iters=8)
+    torch.cuda.synchronize()
+    assert n_fma == out.numel() * 8 * 128
+    assert torch.isfinite(out).all()
