@@ -243,6 +243,35 @@ RUBIX_API int rubix_fits_cube_layout(const float* cube, int32_t A, int32_t B, in
                                      int64_t spaxel_stride, void* out, void* stream);
 
 /*
+ * rubix_psf_fwd and rubix_lsf_fwd with the taps in device memory (ty, tx, taps are
+ * device pointers of m_y, m_x, n_taps floats), so that taps computed on the device
+ * (rubix_gauss_taps) need no copy to the host.  Same arguments, limits and results.
+ */
+RUBIX_API int rubix_psf_fwd_dtaps(const float* in, float* out, int32_t ny, int32_t nx,
+                                  int32_t n_wave_t, int64_t spaxel_stride_in,
+                                  int64_t spaxel_stride_out, const float* ty, int32_t m_y,
+                                  const float* tx, int32_t m_x, void* stream);
+RUBIX_API int rubix_lsf_fwd_dtaps(const float* in, float* out, int64_t n_rows,
+                                  int32_t n_wave_t, int64_t row_stride_in,
+                                  int64_t row_stride_out, const float* taps, int32_t n_taps,
+                                  int32_t crop, void* stream);
+
+/*
+ * Replaces, for a sigma held on the device, the tap computation of rubix's
+ * gaussian_kernel_2d (telescope/psf/kernels.py:5-31; the 2-D kernel is the outer product
+ * of these 1-D taps) and of the LSF kernel (telescope/lsf/lsf.py:12-26), plus the
+ * derivative jax.grad takes through them.
+ *
+ * sigma: one double in device memory; x: m positions (host, copied by value, m < 64).
+ * taps[i] = e_i / sum e with e_i = exp(-x_i^2 / (2 sigma^2)); dtaps (optional) = d taps /
+ * d sigma; rtaps (optional) = taps reversed, followed by one zero when rtaps_pad (the
+ * adjoint taps of a 'same' convolution with even m).  float64 arithmetic, float32
+ * results, all in device memory; one launch, no synchronisation.
+ */
+RUBIX_API int rubix_gauss_taps(const double* sigma, const double* x, int32_t m, float* taps,
+                               float* dtaps, float* rtaps, int32_t rtaps_pad, void* stream);
+
+/*
  * No counterpart in rubix (a measurement aid).
  *
  * rubix_fma_probe_blocks() blocks of 256 threads each run iters * 128 dependent-chain

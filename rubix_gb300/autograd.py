@@ -21,7 +21,9 @@ transmission in both passes; A_V itself is held fixed (no gradient to the coordi
 or the gas).  Gradients flow to the particle
 inputs (velocity: the line-of-sight component only) and to ``sigma_psf`` /
 ``sigma_lsf`` given as tensors; the spaxel assignment (coordinates) is piecewise
-constant and gets none, as in rubix.
+constant and gets none, as in rubix.  For sigmas given as CUDA tensors the taps and
+their derivatives are computed on the device (``rubix_gauss_taps``) and read there by
+the PSF/LSF kernels, so a step never reads a value back to the host.
 """
 
 from __future__ import annotations
@@ -64,8 +66,30 @@ def _psf_adjoint_taps(t: np.ndarray) -> np.ndarray:
     return r if r.size % 2 == 1 else np.concatenate([r, [0.0]])
 
 
-def _scalar(x) -> float:
-    return float(x.detach().item()) if isinstance(x, torch.Tensor) else float(x)
+def _psf_positions(m: int) -> np.ndarray:
+    return np.arange(-((m - 1) / 2), ((m - 1) / 2) + 1)
+
+
+def _lsf_positions(wave_res: float, factor: int = 12) -> np.ndarray:
+    return np.arange(-factor * wave_res, factor * wave_res + wave_res, wave_res,
+                     dtype=np.float32).astype(np.float64)
+
+
+def _psf_taps(sigma, m: int):
+    """(taps, dtaps, adjoint taps): on the device from a CUDA sigma tensor (no read-back
+    of sigma), else on the host."""
+    if isinstance(sigma, torch.Tensor) and sigma.is_cuda:
+        return ops.gauss_taps(sigma, _psf_positions(m), reversed_pad=(m % 2 == 0))
+    t, dt = psf_taps_grad(m, float(sigma))
+    return t, dt, _psf_adjoint_taps(t)
+
+
+def _lsf_taps(sigma, wave_res: float):
+    """(taps, dtaps, reversed taps) of the LSF, on the device for a CUDA sigma tensor."""
+    if isinstance(sigma, torch.Tensor) and sigma.is_cuda:
+        return ops.gauss_taps(sigma, _lsf_positions(wave_res))
+    t, dt = lsf_taps_grad(float(sigma), wave_res)
+    return t, dt, t[::-1].copy()
 
 
 class DatacubeFunction(torch.autograd.Function):
@@ -85,17 +109,16 @@ class DatacubeFunction(torch.autograd.Function):
         A = ops.cube_forward(r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t,
                              mass, metallicity, age, velocity, r.velocity_axis, perm,
                              seg_offsets, nseg, dust_av=dust_av, dust_exponent=dust_e)
-        sp, sl = _scalar(sigma_psf), _scalar(sigma_lsf)
-        tl, _ = lsf_taps_grad(sl, wave_res)
-        crop = (tl.size - 1) // 2
-        Q = ops.lsf_forward(A, tl, crop)
-        tp, _ = psf_taps_grad(int(psf_size), sp)
-        cube = ops.psf_forward(Q.view(r.sbin, r.sbin, -1), tp)
+        lsf_t = _lsf_taps(sigma_lsf, wave_res)
+        psf_t = _psf_taps(sigma_psf, int(psf_size))
+        crop = (len(lsf_t[0]) - 1) // 2
+        Q = ops.lsf_forward(A, lsf_t[0], crop)
+        cube = ops.psf_forward(Q.view(r.sbin, r.sbin, -1), psf_t[0])
         ctx.save_for_backward(mass, metallicity, age, velocity, A, Q)
         ctx.r = r
         ctx.perm, ctx.seg_offsets = perm, seg_offsets
         ctx.dust = (dust_av, dust_e)
-        ctx.sp, ctx.sl, ctx.psf_size, ctx.wave_res = sp, sl, int(psf_size), wave_res
+        ctx.lsf_t, ctx.psf_t, ctx.crop = lsf_t, psf_t, crop
         ctx.sigma_dtypes = (
             sigma_psf.dtype if isinstance(sigma_psf, torch.Tensor) else None,
             sigma_lsf.dtype if isinstance(sigma_lsf, torch.Tensor) else None)
@@ -107,14 +130,14 @@ class DatacubeFunction(torch.autograd.Function):
         r = ctx.r
         nseg = r.sbin * r.sbin
         g = g.contiguous().float()
-        tp, dtp = psf_taps_grad(ctx.psf_size, ctx.sp)
-        tl, dtl = lsf_taps_grad(ctx.sl, ctx.wave_res)
-        crop = (tl.size - 1) // 2
-        gP = ops.psf_forward(g, _psf_adjoint_taps(tp))
+        tp, dtp, rtp = ctx.psf_t
+        tl, dtl, rtl = ctx.lsf_t
+        crop = ctx.crop
+        gP = ops.psf_forward(g, rtp)
         need = ctx.needs_input_grad
         grads = [None] * 12
         if any(need[:4]):
-            h = ops.lsf_forward(gP, tl[::-1].copy(), tl.size - 1 - crop)
+            h = ops.lsf_forward(gP, rtl, len(tl) - 1 - crop)
             gm, gz, ga, gv = ops.cube_backward(
                 r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t, mass,
                 metallicity, age, velocity, r.velocity_axis, ctx.perm, ctx.seg_offsets, nseg,

@@ -21,6 +21,7 @@ struct LsfArgs {
   long long sin, sout;
   int K, crop;
   float taps[kLsfMaxTaps + 1];
+  const float* taps_dev;  // when set, the taps are read from device memory instead
 };
 
 // out[t] = sum_q w[q] * s[t + q] with s[i] = in[i - (K-1-crop)] and w[q] = taps[K-1-q].
@@ -29,7 +30,8 @@ __global__ void __launch_bounds__(kLsfThreads) lsf_vec_kernel(LsfArgs a) {
   extern __shared__ __align__(16) float s_row[];
   __shared__ float s_w[KC * 4];
   const int tid = threadIdx.x;
-  for (int q = tid; q < KC * 4; q += kLsfThreads) s_w[q] = (q < a.K) ? a.taps[a.K - 1 - q] : 0.f;
+  const float* tp = a.taps_dev ? a.taps_dev : a.taps;
+  for (int q = tid; q < KC * 4; q += kLsfThreads) s_w[q] = (q < a.K) ? tp[a.K - 1 - q] : 0.f;
   const int lead = a.K - 1 - a.crop;           // zeros before in[0]
   const int n4 = (a.n + 3) / 4;                 // output groups of 4
   const int span = n4 * 4 + KC * 4;             // staged length (multiple of 4)
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(kLsfThreads) lsf_scalar_kernel(LsfArgs a) {
   extern __shared__ __align__(16) float s_row[];
   __shared__ float s_w[kLsfMaxTaps + 1];
   const int tid = threadIdx.x;
-  for (int q = tid; q < a.K; q += kLsfThreads) s_w[q] = a.taps[a.K - 1 - q];
+  const float* tp = a.taps_dev ? a.taps_dev : a.taps;
+  for (int q = tid; q < a.K; q += kLsfThreads) s_w[q] = tp[a.K - 1 - q];
   const int lead = a.K - 1 - a.crop;
   const int span = a.n + a.K - 1;
   for (long long row = blockIdx.x; row < a.rows; row += gridDim.x) {
@@ -115,9 +118,12 @@ int launch_vec(const LsfArgs& a, cudaStream_t st) {
 
 using namespace rubix;
 
-extern "C" int rubix_lsf_fwd(const float* in, float* out, int64_t n_rows, int32_t n_wave_t,
-                             int64_t row_stride_in, int64_t row_stride_out, const float* taps,
-                             int32_t n_taps, int32_t crop, void* stream) {
+namespace rubix {
+namespace {
+
+int lsf_fwd_impl(const float* in, float* out, int64_t n_rows, int32_t n_wave_t,
+                 int64_t row_stride_in, int64_t row_stride_out, const float* taps,
+                 int32_t n_taps, int32_t crop, bool device_taps, void* stream) {
   RUBIX_REQUIRE(n_rows >= 0 && n_wave_t >= 0, RUBIX_E_SHAPE, "rubix_lsf_fwd: negative size");
   RUBIX_REQUIRE(n_taps >= 1 && n_taps <= kLsfMaxTaps, RUBIX_E_SHAPE,
                 "rubix_lsf_fwd: n_taps must be in [1, %d]", kLsfMaxTaps);
@@ -139,7 +145,8 @@ extern "C" int rubix_lsf_fwd(const float* in, float* out, int64_t n_rows, int32_
   a.sout = row_stride_out;
   a.K = n_taps;
   a.crop = crop;
-  for (int i = 0; i <= kLsfMaxTaps; ++i) a.taps[i] = i < n_taps ? taps[i] : 0.f;
+  a.taps_dev = device_taps ? taps : nullptr;
+  for (int i = 0; i <= kLsfMaxTaps; ++i) a.taps[i] = (!device_taps && i < n_taps) ? taps[i] : 0.f;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // KC = ceil(K/4) weight chunks; each thread's window is KC+1 float4 loads.
   switch ((n_taps + 3) / 4) {
@@ -160,4 +167,22 @@ extern "C" int rubix_lsf_fwd(const float* in, float* out, int64_t n_rows, int32_
   lsf_scalar_kernel<<<(int)grid, kLsfThreads, smem, st>>>(a);
   RUBIX_LAUNCH_CHECK("lsf_scalar_kernel");
   return RUBIX_OK;
+}
+
+}  // namespace
+}  // namespace rubix
+
+extern "C" int rubix_lsf_fwd(const float* in, float* out, int64_t n_rows, int32_t n_wave_t,
+                             int64_t row_stride_in, int64_t row_stride_out, const float* taps,
+                             int32_t n_taps, int32_t crop, void* stream) {
+  return lsf_fwd_impl(in, out, n_rows, n_wave_t, row_stride_in, row_stride_out, taps, n_taps,
+                      crop, false, stream);
+}
+
+extern "C" int rubix_lsf_fwd_dtaps(const float* in, float* out, int64_t n_rows,
+                                   int32_t n_wave_t, int64_t row_stride_in,
+                                   int64_t row_stride_out, const float* taps, int32_t n_taps,
+                                   int32_t crop, void* stream) {
+  return lsf_fwd_impl(in, out, n_rows, n_wave_t, row_stride_in, row_stride_out, taps, n_taps,
+                      crop, true, stream);
 }

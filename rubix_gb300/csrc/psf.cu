@@ -30,6 +30,8 @@ struct PsfArgs {
   int my, mx, oy, ox;
   float ty[kMaxTaps + 1];
   float tx[kMaxTaps + 1];
+  const float* ty_dev;  // when set, the taps are read from device memory instead
+  const float* tx_dev;
 };
 
 __global__ void __launch_bounds__(kPsfThreads) psf_strip_kernel(PsfArgs a) {
@@ -39,8 +41,8 @@ __global__ void __launch_bounds__(kPsfThreads) psf_strip_kernel(PsfArgs a) {
   float* s_ring = smem + wrow * kPsfTileL;  // [my][kPsfTileX][kPsfTileL]
   __shared__ float s_ty[kMaxTaps + 1], s_tx[kMaxTaps + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid < a.my) s_ty[tid] = a.ty[tid];
-  if (tid < a.mx) s_tx[tid] = a.tx[tid];
+  if (tid < a.my) s_ty[tid] = a.ty_dev ? a.ty_dev[tid] : a.ty[tid];
+  if (tid < a.mx) s_tx[tid] = a.tx_dev ? a.tx_dev[tid] : a.tx[tid];
   const int x0 = blockIdx.x * kPsfTileX;
   const int l0 = blockIdx.y * kPsfTileL;
   const int l = l0 + lane;
@@ -226,8 +228,9 @@ __device__ __forceinline__ void psf_reg_body(const float* __restrict__ in, float
 
 template <int M>
 __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
-  psf_reg_body<M>(a.in, a.out, a.ny, a.nx, a.nl, a.sin, a.sout, a.oy, a.ox, a.ty, a.tx,
-                  blockIdx.x, blockIdx.y);
+  psf_reg_body<M>(a.in, a.out, a.ny, a.nx, a.nl, a.sin, a.sout, a.oy, a.ox,
+                  a.ty_dev ? a.ty_dev : a.ty, a.tx_dev ? a.tx_dev : a.tx, blockIdx.x,
+                  blockIdx.y);
 }
 
 // Ragged batch: galaxy g owns blocks [block_off[g], block_off[g+1]) (x strips fastest),
@@ -276,19 +279,23 @@ int launch_psf_reg(const PsfArgs& a, cudaStream_t st) {
 
 using namespace rubix;
 
-extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx,
-                             int32_t n_wave_t, int64_t spaxel_stride_in,
-                             int64_t spaxel_stride_out, const float* ty, int32_t m_y,
-                             const float* tx, int32_t m_x, void* stream) {
-  RUBIX_REQUIRE(ny >= 0 && nx >= 0 && n_wave_t >= 0, RUBIX_E_SHAPE, "rubix_psf_fwd: negative size");
+namespace rubix {
+namespace {
+
+int psf_fwd_impl(const float* in, float* out, int32_t ny, int32_t nx, int32_t n_wave_t,
+                 int64_t spaxel_stride_in, int64_t spaxel_stride_out, const float* ty,
+                 int32_t m_y, const float* tx, int32_t m_x, bool device_taps, void* stream) {
+  const char* sfx = device_taps ? "_dtaps" : "";
+  RUBIX_REQUIRE(ny >= 0 && nx >= 0 && n_wave_t >= 0, RUBIX_E_SHAPE,
+                "rubix_psf_fwd%s: negative size", sfx);
   RUBIX_REQUIRE(m_y >= 1 && m_y <= 31 && m_x >= 1 && m_x <= kMaxTaps, RUBIX_E_SHAPE,
-                "rubix_psf_fwd: kernel sizes must satisfy 1 <= m_y <= 31, 1 <= m_x <= %d",
+                "rubix_psf_fwd%s: kernel sizes must satisfy 1 <= m_y <= 31, 1 <= m_x <= %d", sfx,
                 kMaxTaps);
   RUBIX_REQUIRE(spaxel_stride_in >= n_wave_t && spaxel_stride_out >= n_wave_t, RUBIX_E_SHAPE,
-                "rubix_psf_fwd: spaxel stride smaller than n_wave_t");
+                "rubix_psf_fwd%s: spaxel stride smaller than n_wave_t", sfx);
   if (ny == 0 || nx == 0 || n_wave_t == 0) return RUBIX_OK;
-  RUBIX_REQUIRE(in && out && ty && tx, RUBIX_E_INVALID, "rubix_psf_fwd: null pointer");
-  RUBIX_REQUIRE(in != out, RUBIX_E_INVALID, "rubix_psf_fwd: in and out must differ");
+  RUBIX_REQUIRE(in && out && ty && tx, RUBIX_E_INVALID, "rubix_psf_fwd%s: null pointer", sfx);
+  RUBIX_REQUIRE(in != out, RUBIX_E_INVALID, "rubix_psf_fwd%s: in and out must differ", sfx);
   PsfArgs a;
   a.in = in;
   a.out = out;
@@ -301,9 +308,11 @@ extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx
   a.mx = m_x;
   a.oy = (m_y - 1) / 2;
   a.ox = (m_x - 1) / 2;
+  a.ty_dev = device_taps ? ty : nullptr;
+  a.tx_dev = device_taps ? tx : nullptr;
   for (int i = 0; i <= kMaxTaps; ++i) {
-    a.ty[i] = i < m_y ? ty[i] : 0.f;
-    a.tx[i] = i < m_x ? tx[i] : 0.f;
+    a.ty[i] = (!device_taps && i < m_y) ? ty[i] : 0.f;
+    a.tx[i] = (!device_taps && i < m_x) ? tx[i] : 0.f;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the register kernel keeps per-row element offsets in 32 bits
@@ -334,6 +343,25 @@ extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx
   psf_strip_kernel<<<grid, kPsfThreads, smem, st>>>(a);
   RUBIX_LAUNCH_CHECK("psf_strip_kernel");
   return RUBIX_OK;
+}
+
+}  // namespace
+}  // namespace rubix
+
+extern "C" int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx,
+                             int32_t n_wave_t, int64_t spaxel_stride_in,
+                             int64_t spaxel_stride_out, const float* ty, int32_t m_y,
+                             const float* tx, int32_t m_x, void* stream) {
+  return psf_fwd_impl(in, out, ny, nx, n_wave_t, spaxel_stride_in, spaxel_stride_out, ty, m_y,
+                      tx, m_x, false, stream);
+}
+
+extern "C" int rubix_psf_fwd_dtaps(const float* in, float* out, int32_t ny, int32_t nx,
+                                   int32_t n_wave_t, int64_t spaxel_stride_in,
+                                   int64_t spaxel_stride_out, const float* ty, int32_t m_y,
+                                   const float* tx, int32_t m_x, void* stream) {
+  return psf_fwd_impl(in, out, ny, nx, n_wave_t, spaxel_stride_in, spaxel_stride_out, ty, m_y,
+                      tx, m_x, true, stream);
 }
 
 extern "C" int rubix_ragged_psf_fwd(const float* in, float* out, int32_t n_wave_t,

@@ -360,16 +360,29 @@ def _host_taps(t) -> np.ndarray:
     return a
 
 
+def _is_device_taps(t) -> bool:
+    return isinstance(t, torch.Tensor) and t.is_cuda
+
+
 def psf_forward(cube: torch.Tensor, taps_y, taps_x=None, out=None) -> torch.Tensor:
-    """Separable 'same' convolution of every wavelength plane of cube [ny, nx, L]."""
+    """Separable 'same' convolution of every wavelength plane of cube [ny, nx, L].  Taps
+    on the host (array-like) or, both, as float32 CUDA tensors (no host copy)."""
     _check_cuda("cube", cube, torch.float32)
     if cube.dim() != 3 or cube.stride(2) != 1 or cube.stride(0) != cube.shape[1] * cube.stride(1):
         cube = cube.contiguous()
     ny, nx, L = cube.shape
-    ty = _host_taps(taps_y)
-    tx = ty if taps_x is None else _host_taps(taps_x)
     if out is None:
         out = torch.empty((ny, nx, L), dtype=torch.float32, device=cube.device)
+    if _is_device_taps(taps_y):
+        ty = _contig("taps_y", taps_y, torch.float32).reshape(-1)
+        tx = ty if taps_x is None else _contig("taps_x", taps_x, torch.float32).reshape(-1)
+        _lib.call("rubix_psf_fwd_dtaps", _ptr(cube), _ptr(out), ny, nx, L, cube.stride(1),
+                  out.stride(1), _ptr(ty), ty.numel(), _ptr(tx), tx.numel(),
+                  _stream(cube.device))
+        _count(1 if cube.numel() > 0 else 0)
+        return out
+    ty = _host_taps(taps_y)
+    tx = ty if taps_x is None else _host_taps(taps_x)
     _lib.call("rubix_psf_fwd", _ptr(cube), _ptr(out), ny, nx, L, cube.stride(1), out.stride(1),
               ty.ctypes.data, ty.size, tx.ctypes.data, tx.size, _stream(cube.device))
     _count(1 if cube.numel() > 0 else 0)
@@ -383,10 +396,17 @@ def lsf_forward(cube: torch.Tensor, taps, crop: int, out=None) -> torch.Tensor:
         cube = cube.contiguous()
     L = cube.shape[-1]
     rows = cube.reshape(-1, L) if cube.is_contiguous() else cube.contiguous().reshape(-1, L)
-    k = _host_taps(taps)
     if out is None:
         out = torch.empty(cube.shape, dtype=torch.float32, device=cube.device)
     orow = out.view(-1, L)
+    if _is_device_taps(taps):
+        k = _contig("taps", taps, torch.float32).reshape(-1)
+        _lib.call("rubix_lsf_fwd_dtaps", _ptr(rows), _ptr(orow), rows.shape[0], L,
+                  rows.stride(0), orow.stride(0), _ptr(k), k.numel(), int(crop),
+                  _stream(cube.device))
+        _count(1 if cube.numel() > 0 else 0)
+        return out
+    k = _host_taps(taps)
     _lib.call("rubix_lsf_fwd", _ptr(rows), _ptr(orow), rows.shape[0], L, rows.stride(0),
               orow.stride(0), k.ctypes.data, k.size, int(crop), _stream(cube.device))
     _count(1 if cube.numel() > 0 else 0)
@@ -545,6 +565,25 @@ def fits_cube_layout(cube: torch.Tensor, out=None) -> torch.Tensor:
               _stream(cube.device))
     _count(1 if A * B * L > 0 else 0)
     return out
+
+
+def gauss_taps(sigma: torch.Tensor, x, reversed_pad: bool = False):
+    """(taps, dtaps/dsigma, reversed taps) float32 CUDA tensors of the normalised Gaussian
+    at positions ``x`` (host array) for a sigma held on the device (0-d tensor): no
+    synchronisation (``rubix_gauss_taps``).  The reversed taps get a trailing zero when
+    ``reversed_pad``."""
+    _check_cuda("sigma", sigma, None)
+    sg = sigma.detach().to(torch.float64).reshape(1).contiguous()
+    xs = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1))
+    m = xs.size
+    dev = sg.device
+    taps = torch.empty(m, dtype=torch.float32, device=dev)
+    dtaps = torch.empty(m, dtype=torch.float32, device=dev)
+    rtaps = torch.empty(m + (1 if reversed_pad else 0), dtype=torch.float32, device=dev)
+    _lib.call("rubix_gauss_taps", _ptr(sg), xs.ctypes.data, m, _ptr(taps), _ptr(dtaps),
+              _ptr(rtaps), 1 if reversed_pad else 0, _stream(dev))
+    _count(1)
+    return taps, dtaps, rtaps
 
 
 def fma_probe(device, iters: int = 4096):

@@ -132,3 +132,74 @@ def test_backward_deterministic():
     torch.cuda.synchronize()
     for a, b in zip(*outs):
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("m", [1, 4, 11, 15, 16])
+def test_device_taps_match_host(m):
+    """rubix_gauss_taps (sigma on the device) gives the host taps, derivatives and
+    adjoint taps of the PSF and LSF."""
+    import torch
+
+    from rubix_gb300 import autograd as ag
+    from rubix_gb300 import ops
+
+    for sigma in (0.7, 1.5, 3.0):
+        sg = torch.tensor(sigma, dtype=torch.float64, device="cuda")
+        t, dt, rt = (x.cpu().numpy() for x in ops.gauss_taps(sg, ag._psf_positions(m),
+                                                            reversed_pad=(m % 2 == 0)))
+        ht, hdt = ag.psf_taps_grad(m, sigma)
+        np.testing.assert_allclose(t, ht, rtol=1e-6, atol=1e-9)
+        np.testing.assert_allclose(dt, hdt, rtol=1e-5, atol=1e-8)
+        np.testing.assert_allclose(rt, ag._psf_adjoint_taps(ht), rtol=1e-6, atol=1e-9)
+    sg = torch.tensor(1.2, dtype=torch.float64, device="cuda")
+    t, dt, rt = (x.cpu().numpy() for x in ops.gauss_taps(sg, ag._lsf_positions(1.25)))
+    ht, hdt = ag.lsf_taps_grad(1.2, 1.25)
+    np.testing.assert_allclose(t, ht, rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(dt, hdt, rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(rt, ht[::-1], rtol=1e-6, atol=1e-9)
+
+
+def test_sigma_tensors_need_no_readback(grad_case):
+    """With CUDA sigma tensors the forward and backward issue no device-to-host copy:
+    the same gradients come out when the stream is captured in a CUDA graph (a capture
+    fails on any synchronising call)."""
+    import torch
+
+    from rubix_gb300.api import IFURenderer
+    from rubix_gb300.autograd import render_cube
+
+    w, W, got = grad_case
+    p = w.particles
+    r = IFURenderer.from_workload(w, psf=False, lsf=False)
+    coords = to_dev(p.coords)
+    mass = to_dev(p.mass).requires_grad_()
+    met, age, vel = to_dev(p.metallicity), to_dev(p.age), to_dev(p.velocity)
+    sp = torch.tensor(w.psf_sigma, dtype=torch.float64, device="cuda", requires_grad=True)
+    sl = torch.tensor(w.lsf_sigma, dtype=torch.float64, device="cuda", requires_grad=True)
+    Wd = to_dev(W).double()
+    idx, mask = r.assign(coords)
+    perm, offs = r.sort(idx, mask)
+    from rubix_gb300.autograd import DatacubeFunction
+
+    def step():
+        cube = DatacubeFunction.apply(mass, met, age, vel, sp, sl, r, perm, offs, w.psf_size,
+                                      w.wave_res)
+        (cube.double() * Wd).sum().backward()
+
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        step()  # warm-up outside the capture (allocations, library load)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    for t in (mass, sp, sl):
+        t.grad = None
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    g.replay()
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(mass.grad.cpu().numpy(), got["mass"], rtol=1e-5,
+                               atol=1e-6 * float(np.abs(got["mass"]).max()))
+    assert abs(float(sp.grad) - got["sigma_psf"]) <= 1e-5 * abs(got["sigma_psf"])
+    assert abs(float(sl.grad) - got["sigma_lsf"]) <= 1e-5 * abs(got["sigma_lsf"])
