@@ -407,6 +407,58 @@ def dusty_bench(dev, w, d_in, steps, warmup, flush, n_gas=500_000):
                         "broken power-law dust-to-gas ratio (X_CO = Z)"}
 
 
+def pipeline_bench(dev, w, steps, warmup, flush):
+    """The same forward through rubix's step API (RubixPipeline.run: rotate_galaxy,
+    filter_particles, spaxel_assignment, reshape_data, the lazy spectra steps,
+    calculate_datacube, convolve_psf, convolve_lsf, apply_noise) with device-resident
+    inputs; the rotation reads the 3x3 inertia tensor back for the host
+    eigen-decomposition."""
+    import torch
+
+    from rubix_gb300.core import (Galaxy, RubixData, RubixPipeline, StarsData,
+                                  register_ssp_template, register_telescope)
+    from rubix_gb300.core.ssp import SSPGrid
+    from rubix_gb300 import synth
+
+    register_ssp_template("bench_ssp", SSPGrid(age=w.ssp.age, metallicity=w.ssp.metallicity,
+                                               wavelength=w.ssp.wavelength, flux=w.ssp.flux))
+    fov = synth.WORKLOADS[w.name]["fov"]
+    register_telescope("bench_ifu", dict(fov=fov, spatial_res=synth.SPATIAL_RES,
+                                         wave_range=list(synth.WAVE_RANGE),
+                                         wave_res=synth.WAVE_RES, lsf_fwhm=2.51,
+                                         signal_to_noise=None, aperture_type="square",
+                                         pixel_type="square"))
+    cfg = {"pipeline": {"name": "calc_ifu"}, "logger": {"log_level": "WARNING"},
+           "data": {"args": {"particle_type": ["stars"]}},
+           "telescope": {"name": "bench_ifu",
+                         "psf": {"name": "gaussian", "size": w.psf_size, "sigma": w.psf_sigma},
+                         "lsf": {"sigma": w.lsf_sigma},
+                         "noise": {"signal_to_noise": 1e30, "noise_distribution": "normal"}},
+           "cosmology": {"name": "PLANCK15"},
+           "galaxy": {"dist_z": w.dist_z, "rotation": {"type": "face-on"}},
+           "ssp": {"template": {"name": "bench_ssp"}, "method": "linear"}}
+    p = w.particles
+    dev_in = [torch.from_numpy(a).to(dev) for a in (p.coords, p.velocity, p.mass,
+                                                     p.metallicity, p.age)]
+
+    def run():
+        data = RubixData(galaxy=Galaxy(halfmassrad_stars=5.0),
+                         stars=StarsData(coords=dev_in[0], velocity=dev_in[1], mass=dev_in[2],
+                                         metallicity=dev_in[3], age=dev_in[4]))
+        return RubixPipeline(cfg, data).run().stars.datacube
+
+    ms = _time_steps(run, steps, warmup, flush)
+    N, L = p.n, int(w.wave_t.size)
+    return {"metric": "particles*lambda/s, particle->IFU datacube forward through "
+                      "RubixPipeline(config, data).run()",
+            "value": N * L / (ms * 1e-3), "unit": "particle*lambda/s", "ms_per_step": ms,
+            "path": "rotate_galaxy (face-on), filter_particles, spaxel_assignment, "
+                    "reshape_data, calculate_spectra, scale_spectrum_by_mass, "
+                    "doppler_shift_and_resampling, calculate_datacube, convolve_psf, "
+                    "convolve_lsf, apply_noise (S/N 1e30: the noise kernels run, the cube is "
+                    "unchanged in float32)"}
+
+
 def fits_bench(dev, cube, steps, warmup, flush):
     """FITS layout of the final cube (transpose to [lambda][x][y] + big-endian) on the
     GPU: algorithmic bytes 2 C per launch (read + write), against the HBM peak."""
@@ -775,6 +827,7 @@ def main():
                 ("plain_gpu_fwd_bwd", lambda: plain_fwd_bwd_bench(dev, args.steps, 1)),
                 ("dusty", lambda: dusty_bench(dev, w, d_in, args.steps, 3, flush)),
                 ("fits_layout", lambda: fits_bench(dev, ours_final, args.steps, 3, flush)),
+                ("pipeline_api", lambda: pipeline_bench(dev, w, min(args.steps, 5), 3, flush)),
                 ("ragged", lambda: ragged_bench(dev, 3, 2))):
             try:
                 extras[name] = fn()

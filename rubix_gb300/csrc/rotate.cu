@@ -61,14 +61,22 @@ __global__ void __launch_bounds__(kInThreads) inertia_partial_kernel(
   }
 }
 
-__global__ void inertia_finish_kernel(const double* __restrict__ partial, int n_blocks,
-                                      const float* __restrict__ pos,
-                                      const float* __restrict__ mass, long long n,
-                                      double* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double v[kInVals] = {0, 0, 0, 0, 0, 0, 0};
-  for (int b = 0; b < n_blocks; ++b)
-    for (int j = 0; j < kInVals; ++j) v[j] += partial[(long long)b * kInVals + j];
+// Block partials summed by one warp per value (lane-strided, then a fixed shuffle tree:
+// deterministic), then the padding correction and the 3x3 layout by thread 0.
+__global__ void __launch_bounds__(kInVals * 32) inertia_finish_kernel(
+    const double* __restrict__ partial, int n_blocks, const float* __restrict__ pos,
+    const float* __restrict__ mass, long long n, double* __restrict__ out) {
+  __shared__ double s_v[kInVals];
+  const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
+  double acc = 0.0;
+  for (int b = lane; b < n_blocks; b += 32) acc += partial[(long long)b * kInVals + j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) s_v[j] = acc;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double v[kInVals];
+  for (int q = 0; q < kInVals; ++q) v[q] = s_v[q];
   // index padding of jnp.where(..., size=N): particle 0 once more per particle outside
   const double extra = (double)n - v[6];
   if (n > 0 && extra > 0.0) {
@@ -126,7 +134,8 @@ extern "C" int rubix_inertia_tensor(const float* positions, int64_t n, int64_t s
   inertia_partial_kernel<<<kInBlocks, kInThreads, 0, st>>>(positions, stride, masses, n,
                                                           halfmass_radius, partial);
   RUBIX_LAUNCH_CHECK("inertia_partial_kernel");
-  inertia_finish_kernel<<<1, 32, 0, st>>>(partial, kInBlocks, positions, masses, n, out9);
+  inertia_finish_kernel<<<1, kInVals * 32, 0, st>>>(partial, kInBlocks, positions, masses, n,
+                                                    out9);
   RUBIX_LAUNCH_CHECK("inertia_finish_kernel");
   return RUBIX_OK;
 }

@@ -317,7 +317,8 @@ def noise_median(flux: torch.Tensor) -> torch.Tensor:
     ws = workspace(_lib.query("rubix_noise_median_workspace_size"), f.device)
     _lib.call("rubix_noise_median", _ptr(f), f.numel(), _ptr(out), _ptr(ws), ws.numel(),
               _stream(f.device))
-    _count(2 + 8 * (f.numel() > 0))
+    # one block-wide select up to 2^20 values; else init, 8 x (histogram, pick), finish
+    _count(1 if f.numel() <= (1 << 20) else 2 + 16 * (f.numel() > 0))
     return out
 
 
