@@ -699,7 +699,50 @@ def philox4x32_10(counter, key):
     return c
 
 
-__all__ += ["noise_sigma", "philox4x32_10"]
+def philox4x32_10_arrays(c0, c1, c2, c3, k0, k1):
+    """philox4x32_10 over arrays of counters (NumPy uint64 arithmetic, same rounds)."""
+    m = np.uint64(0xFFFFFFFF)
+    c = [np.asarray(x, dtype=np.uint64) & m for x in (c0, c1, c2, c3)]
+    k0, k1 = np.uint64(int(k0) & 0xFFFFFFFF), np.uint64(int(k1) & 0xFFFFFFFF)
+    for _ in range(10):
+        p0 = np.uint64(0xD2511F53) * c[0]
+        p1 = np.uint64(0xCD9E8D57) * c[2]
+        c = [((p1 >> np.uint64(32)) ^ c[1] ^ k0) & m, p1 & m,
+             ((p0 >> np.uint64(32)) ^ c[3] ^ k1) & m, p0 & m]
+        k0 = (k0 + np.uint64(0x9E3779B9)) & m
+        k1 = (k1 + np.uint64(0xBB67AE85)) & m
+    return c
+
+
+def noise_draws(n_spaxels, n_wave, seed, distribution="normal"):
+    """The draws z[s, t] of rubix_apply_noise (float64): element (s, t) has the index
+    e = s * n_wave + t and takes output e % 4 of the Philox4x32-10 call with counter
+    (e // 4 low word, high word, 0, 0) and key (seed low word, high word).  Uniform
+    draws are (bits >> 8) / 2^24; normal draws pair outputs (0, 1) and (2, 3) by
+    Box-Muller, r = sqrt(-2 ln u) with u = ((bits >> 8) + 1) / 2^24 from the first of the
+    pair and the angle 2 pi (u' - 1/2) from the second (cos for the first, sin for the
+    second).  Test infrastructure: the noise of rubix itself (jax.random with a fixed
+    key, telescope/noise/noise.py:103) is matched in distribution only."""
+    e = np.arange(int(n_spaxels) * int(n_wave), dtype=np.uint64)
+    q = e >> np.uint64(2)
+    r = philox4x32_10_arrays(q & np.uint64(0xFFFFFFFF), q >> np.uint64(32), 0, 0,
+                             int(seed) & 0xFFFFFFFF, (int(seed) >> 32) & 0xFFFFFFFF)
+    u = [(x >> np.uint64(8)).astype(np.float64) / 16777216.0 for x in r]
+    if distribution == "uniform":
+        outs = u
+    else:
+        u0 = [((x >> np.uint64(8)).astype(np.float64) + 1.0) / 16777216.0 for x in r]
+        r1 = np.sqrt(-2.0 * np.log(u0[0]))
+        r2 = np.sqrt(-2.0 * np.log(u0[2]))
+        a1 = 2.0 * np.pi * (u[1] - 0.5)
+        a2 = 2.0 * np.pi * (u[3] - 0.5)
+        outs = [r1 * np.cos(a1), r1 * np.sin(a1), r2 * np.cos(a2), r2 * np.sin(a2)]
+    j = (e & np.uint64(3)).astype(np.int64)
+    z = np.choose(j, outs)
+    return z.reshape(int(n_spaxels), int(n_wave))
+
+
+__all__ += ["noise_sigma", "philox4x32_10", "philox4x32_10_arrays", "noise_draws"]
 
 __all__ += ["interp2d_linear_grad", "doppler_grid", "particle_objective", "particle_grads",
             "psf_taps_derivative", "lsf_taps_derivative"]

@@ -26,6 +26,7 @@ from ..logging import get_logger
 from .config import rubix_config
 from .data import RubixData, device_of, flat_particles, has_device_axis, to_device
 from .ssp import get_ssp, lookup_method
+from .lsf import EXTEND_FACTOR
 from .telescope import get_telescope
 
 _AXIS = {"x": 0, "y": 1, "z": 2}
@@ -185,13 +186,15 @@ def get_doppler_shift_and_resampling(config: dict) -> Callable:
     return doppler_shift_and_resampling
 
 
-def get_calculate_datacube(config: dict) -> Callable:
+def get_calculate_datacube(config: dict, lsf_handoff=None) -> Callable:
     """rubix/core/ifu.py:298-341: per-spaxel sum into a [sbin, sbin, n_lambda] cube.
 
     With lazy spectra the fused kernel runs (stable spaxel sort + lookup/mass/Doppler/
     resample/accumulate); with materialised spectra the rows are summed per spaxel.
     Particles outside the aperture (zero mass after ``filter_particles``) contribute
-    exactly 0 and are left out of the sort.
+    exactly 0 and are left out of the sort.  With ``lsf_handoff`` (a
+    ``core.lsf.LsfHandoff`` shared with the run's ``convolve_lsf``) the fused kernel
+    also applies the LSF, and the later ``convolve_lsf`` passes the cube through.
     """
     logger = get_logger(config.get("logger", None))
     telescope = get_telescope(config)
@@ -210,12 +213,17 @@ def get_calculate_datacube(config: dict) -> Callable:
             # filtered particles have zero mass in the lazy record: dropping them is exact
             keep = flat_particles(st.mask, dev, dtype=torch.uint8)
         perm, offs = ops.spaxel_sort(idx, nseg, keep)
+        fuse = lazy and lsf_handoff is not None and lsf_handoff.taps is not None
+        if lsf_handoff is not None:
+            lsf_handoff.pending = fuse
         if lazy:
             flux, zg, ag, _ = spec.ssp.device_arrays(dev)
             cube = ops.cube_forward(flux, zg, ag, spec.wave_z, spec.wave_t, spec.mass,
                                     spec.metallicity, spec.age, spec.velocity,
                                     spec.velocity_axis, perm, offs, nseg, dust_av=spec.dust_av,
-                                    dust_exponent=spec.dust_exponent)
+                                    dust_exponent=spec.dust_exponent,
+                                    lsf_taps=lsf_handoff.taps if fuse else None,
+                                    lsf_crop=EXTEND_FACTOR)
         else:
             rows = _spectra_tensor(spec, dev)
             cube = ops.segment_sum_rows(rows, perm, offs, nseg)

@@ -19,7 +19,7 @@ from .data import RubixData, get_reshape_data
 from .dust import get_extinction
 from .ifu import (get_calculate_datacube, get_calculate_spectra,
                   get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
-from .lsf import get_convolve_lsf
+from .lsf import LsfHandoff, get_convolve_lsf, lsf_fusable
 from .noise import get_apply_noise
 from .psf import get_convolve_psf
 from .rotation import get_galaxy_rotation
@@ -28,7 +28,12 @@ from .telescope import get_filter_particles, get_spaxel_assignment, get_telescop
 
 
 class RubixPipeline:
-    def __init__(self, user_config, data: Optional[RubixData] = None):
+    """``fuse_lsf``: when the pipeline runs convolve_lsf after calculate_datacube with
+    only convolve_psf between them, apply the LSF in the accumulate kernel's epilogue
+    (the two convolutions commute) instead of in a separate pass over the cube."""
+
+    def __init__(self, user_config, data: Optional[RubixData] = None, *,
+                 fuse_lsf: bool = True):
         self.user_config = get_config(user_config)
         self.pipeline_config = get_pipeline_config(self.user_config["pipeline"]["name"])
         self.logger = get_logger(self.user_config.get("logger"))
@@ -38,14 +43,16 @@ class RubixPipeline:
             raise ValueError("rubix_gb300.RubixPipeline needs the particle data (data=RubixData)")
         self.data = data
         self.func = None
+        self.fuse_lsf = fuse_lsf
 
-    def _get_pipeline_functions(self) -> list:
+    def _get_pipeline_functions(self, handoff: Optional[LsfHandoff] = None) -> list:
         c = self.user_config
+        lsf = get_convolve_lsf(c, handoff)
         funcs = [
             get_galaxy_rotation(c), get_filter_particles(c), get_spaxel_assignment(c),
             get_calculate_spectra(c), get_reshape_data(c), get_scale_spectrum_by_mass(c),
-            get_doppler_shift_and_resampling(c), get_calculate_datacube(c),
-            get_convolve_psf(c), get_convolve_lsf(c), get_apply_noise(c),
+            get_doppler_shift_and_resampling(c), get_calculate_datacube(c, handoff),
+            get_convolve_psf(c), lsf, get_apply_noise(c),
         ]
         # rubix builds calculate_extinction for every pipeline (core/pipeline.py:114);
         # here it is built when the configuration has a dust section
@@ -57,6 +64,9 @@ class RubixPipeline:
         t0 = time.time()
         self._pipeline = LinearTransformerPipeline(self.pipeline_config,
                                                    self._get_pipeline_functions())
+        if self.fuse_lsf and lsf_fusable(self._pipeline._names):
+            self._pipeline = LinearTransformerPipeline(
+                self.pipeline_config, self._get_pipeline_functions(LsfHandoff()))
         self.func = self._pipeline.expression
         out = self.func(self.data)
         import torch

@@ -8,13 +8,15 @@
 //   cube[s][t] += cube[s][t] * sigma[s] * z[s][t],   z ~ N(0, 1) or U[0, 1)
 // rubix draws z from jax.random with a fixed key; here z comes from a Philox4x32-10
 // counter-based generator (Salmon, Moraes, Dror and Shaw, SC'11) keyed by a caller
-// seed: with G = ceil(L / 4), element (s, t) takes output t / G of the call with counter
-// (t % G, s, 0, 0) (so that a warp's 32 calls write 32 consecutive elements at a time),
-// and results are reproducible for a seed but not equal to rubix's draws.  Box-Muller uses
-// the hardware log2 / sin / cos approximations (relative errors near 1e-6, far below
-// anything the noise statistics can show).  The median is an exact radix select (four
-// 8-bit passes over the float bit patterns, integer histograms), in one block for up
-// to 2^20 spaxels.
+// seed: element (s, t) has the index e = s * L + t in the unpadded [spaxel][lambda]
+// order and takes output e % 4 of the call with counter (e / 4 as two 32-bit words, 0,
+// 0), so one call serves four consecutive elements (one float4 of an unpadded,
+// 16-byte-aligned cube).  Results are reproducible for a seed but not equal to rubix's
+// draws.  Normal draws pair outputs (0, 1) and (2, 3) by Box-Muller on the hardware
+// log2 / sin / cos approximations (relative errors near 1e-6, far below anything the
+// noise statistics can show).  The median is an exact radix select (four 8-bit passes
+// over the float bit patterns, integer histograms), in one block for up to 2^20
+// spaxels.
 #include <math.h>
 
 #include "common.cuh"
@@ -195,45 +197,81 @@ __global__ void select_init_kernel(SelectState* __restrict__ st, long long n) {
 }
 
 // ---------------------------------------------------------------- noise
-__global__ void noise_kernel(float* __restrict__ cube, long long n_spaxels, int L,
-                             long long stride, const float* __restrict__ flux,
-                             const float* __restrict__ median, float inv_s2n, int distribution,
-                             uint32_t k0, uint32_t k1) {
-  const float sqm = sqrtf(*median);
-  const int groups = (L + 3) / 4;  // Philox calls per spaxel row
-  const float two_pi = 6.283185307179586f;
-  for (long long s = blockIdx.y; s < n_spaxels; s += gridDim.y) {
+// The four draws of one Philox call.
+__device__ __forceinline__ void quad_draws(U4 r, int distribution, float z[4]) {
+  if (distribution == 0) {  // Box-Muller on two pairs
+    const float two_pi = 6.283185307179586f;
+    const float u1 = u01_open0(r.x), u2 = u01(r.y), u3 = u01_open0(r.z), u4 = u01(r.w);
+    const float r1 = sqrtf(-2.0f * __logf(u1)), r2 = sqrtf(-2.0f * __logf(u3));
+    float s1, c1, s2, c2;
+    // angles in [-pi, pi): the argument range of the hardware approximations
+    __sincosf(two_pi * (u2 - 0.5f), &s1, &c1);
+    __sincosf(two_pi * (u4 - 0.5f), &s2, &c2);
+    z[0] = r1 * c1;
+    z[1] = r1 * s1;
+    z[2] = r2 * c2;
+    z[3] = r2 * s2;
+  } else {
+    z[0] = u01(r.x);
+    z[1] = u01(r.y);
+    z[2] = u01(r.z);
+    z[3] = u01(r.w);
+  }
+}
+
+constexpr int kNoiseThreads = 256;
+constexpr int kNoiseQuads = 4;  // Philox calls per thread per pass over a row
+
+// Blocks stride over spaxel rows; a pass over a row covers kNoiseThreads * kNoiseQuads
+// consecutive quads (calls), with all of a thread's float4 loads issued before its
+// Philox arithmetic.  Quads that straddle the row's ends (and every quad when the
+// cube is padded or not 16-byte aligned) update their elements of this row one by one.
+__global__ void __launch_bounds__(kNoiseThreads) noise_kernel(
+    float* __restrict__ cube, long long n_spaxels, int L, long long stride,
+    const float* __restrict__ flux, const float* __restrict__ median, float inv_s2n,
+    int distribution, uint32_t k0, uint32_t k1, int vec) {
+  const float scale = sqrtf(*median) * inv_s2n;
+  for (long long s = blockIdx.x; s < n_spaxels; s += gridDim.x) {
     const float f = flux[s];
-    const float sig = f > 0.f ? sqm * inv_s2n / sqrtf(f) : 0.f;
+    const float sig = f > 0.f ? scale / sqrtf(f) : 0.f;
+    const long long e0 = s * (long long)L;  // logical index of the row's first element
+    const long long qa = e0 >> 2, qb = (e0 + L - 1) >> 2;  // quads touching the row
     float* row = cube + s * stride;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < groups;
-         g += gridDim.x * blockDim.x) {
-      const U4 r = philox4x32_10(U4{(uint32_t)g, (uint32_t)s, (uint32_t)(s >> 32), 0u}, k0,
-                                 k1);
-      float z[4];
-      if (distribution == 0) {  // Box-Muller on two pairs
-        const float u1 = u01_open0(r.x), u2 = u01(r.y), u3 = u01_open0(r.z), u4 = u01(r.w);
-        const float r1 = sqrtf(-2.0f * __logf(u1)), r2 = sqrtf(-2.0f * __logf(u3));
-        float s1, c1, s2, c2;
-        // angles in [-pi, pi): the argument range of the hardware approximations
-        __sincosf(two_pi * (u2 - 0.5f), &s1, &c1);
-        __sincosf(two_pi * (u4 - 0.5f), &s2, &c2);
-        z[0] = r1 * c1;
-        z[1] = r1 * s1;
-        z[2] = r2 * c2;
-        z[3] = r2 * s2;
-      } else {
-        z[0] = u01(r.x);
-        z[1] = u01(r.y);
-        z[2] = u01(r.z);
-        z[3] = u01(r.w);
+    for (long long base = qa; base <= qb; base += kNoiseThreads * kNoiseQuads) {
+      float4 c[kNoiseQuads];
+      bool whole[kNoiseQuads];
+#pragma unroll
+      for (int k = 0; k < kNoiseQuads; ++k) {
+        const long long q = base + threadIdx.x + k * kNoiseThreads;
+        const long long tq = 4 * q - e0;  // row position of the quad's first element
+        whole[k] = vec && q <= qb && tq >= 0 && tq + 4 <= L;
+        // vec: stride == L and a 16-byte aligned cube, so row + tq == cube + 4 q
+        if (whole[k]) c[k] = *reinterpret_cast<const float4*>(row + tq);
       }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int t = g + j * groups;  // consecutive threads: consecutive elements
-        if (t < L) {
-          const float c = row[t];
-          row[t] = c + c * (sig * z[j]);
+      for (int k = 0; k < kNoiseQuads; ++k) {
+        const long long q = base + threadIdx.x + k * kNoiseThreads;
+        if (q > qb) continue;
+        float z[4];
+        quad_draws(philox4x32_10(U4{(uint32_t)q, (uint32_t)(q >> 32), 0u, 0u}, k0, k1),
+                   distribution, z);
+        const long long tq = 4 * q - e0;
+        if (whole[k]) {
+          float4 v = c[k];
+          v.x = v.x + v.x * (sig * z[0]);
+          v.y = v.y + v.y * (sig * z[1]);
+          v.z = v.z + v.z * (sig * z[2]);
+          v.w = v.w + v.w * (sig * z[3]);
+          *reinterpret_cast<float4*>(row + tq) = v;
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const long long t = tq + j;
+            if (t >= 0 && t < L) {
+              const float v = row[t];
+              row[t] = v + v * (sig * z[j]);
+            }
+          }
         }
       }
     }
@@ -309,12 +347,17 @@ extern "C" int rubix_apply_noise(float* cube, int64_t n_spaxels, int32_t n_wave_
   if (n_spaxels == 0 || n_wave_t == 0) return RUBIX_OK;
   RUBIX_REQUIRE(cube && flux && median, RUBIX_E_INVALID, "rubix_apply_noise: null pointer");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // x: the Philox calls of a spaxel row; y: spaxel rows (grid-strided beyond 65535)
-  const int gx = div_up((n_wave_t + 3) / 4, 256);
-  const unsigned gy = (unsigned)std::min<long long>(n_spaxels, 65535LL);
-  noise_kernel<<<dim3(gx, gy), 256, 0, st>>>(cube, n_spaxels, n_wave_t, spaxel_stride, flux,
-                                             median, 1.0f / signal_to_noise, distribution,
-                                             (uint32_t)seed, (uint32_t)(seed >> 32));
+  static int blocks_per_sm = 0;
+  if (blocks_per_sm == 0) {
+    RUBIX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, noise_kernel,
+                                                                 kNoiseThreads, 0));
+    blocks_per_sm = std::max(blocks_per_sm, 1);
+  }
+  const int grid = (int)std::min<long long>(n_spaxels, (long long)sm_count() * blocks_per_sm);
+  const int vec = spaxel_stride == n_wave_t && (reinterpret_cast<uintptr_t>(cube) & 15) == 0;
+  noise_kernel<<<grid, kNoiseThreads, 0, st>>>(cube, n_spaxels, n_wave_t, spaxel_stride, flux,
+                                               median, 1.0f / signal_to_noise, distribution,
+                                               (uint32_t)seed, (uint32_t)(seed >> 32), vec);
   RUBIX_LAUNCH_CHECK("noise_kernel");
   return RUBIX_OK;
 }

@@ -55,12 +55,15 @@ def _oracle_pipeline(w):
                               rotation=(HALFMASS_RADIUS, 0.0, 0.0, 0.0))
 
 
-def test_rubix_pipeline_matches_oracle():
+@pytest.mark.parametrize("fuse_lsf", [True, False])
+def test_rubix_pipeline_matches_oracle(fuse_lsf):
+    """The LSF in the accumulate epilogue (default) or as its own step: both match."""
     from rubix_gb300.core import RubixPipeline
 
     w = workload("small")
     ref = _oracle_pipeline(w)
-    out = RubixPipeline(_config(w), _data(w)).run()
+    pipe = RubixPipeline(_config(w), _data(w), fuse_lsf=fuse_lsf)
+    out = pipe.run()
     cube = out.stars.datacube.cpu().numpy()
     assert cube.shape == (25, 25, 3721)
     assert_cube_close(cube, ref["final"], what="RubixPipeline cube")

@@ -163,3 +163,17 @@ def test_renderer_and_pipeline_need_cuda_and_data():
            "ssp": {"template": {"name": "synthetic"}, "method": "linear"}}
     with pytest.raises(ValueError, match="needs the particle data"):
         RubixPipeline(cfg)
+
+
+def test_lsf_fusable_order():
+    from rubix_gb300.core.lsf import lsf_fusable
+
+    calc_ifu = ["rotate_galaxy", "filter_particles", "spaxel_assignment", "calculate_spectra",
+                "reshape_data", "scale_spectrum_by_mass", "doppler_shift_and_resampling",
+                "calculate_datacube", "convolve_psf", "convolve_lsf", "apply_noise"]
+    assert lsf_fusable(calc_ifu)
+    assert lsf_fusable(["calculate_datacube", "convolve_lsf", "convolve_psf"])
+    # a step between them that is not the PSF (noise does not commute with the LSF)
+    assert not lsf_fusable(["calculate_datacube", "apply_noise", "convolve_lsf"])
+    assert not lsf_fusable(["convolve_lsf", "calculate_datacube"])
+    assert not lsf_fusable(["calculate_datacube", "convolve_psf"])

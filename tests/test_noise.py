@@ -27,6 +27,27 @@ def test_library_philox_matches_restatement(rubix_lib):
         assert ops.philox4x32_10(c, k) == oracle.philox4x32_10(c, k)
 
 
+def test_vectorised_philox_matches_restatement():
+    rng = np.random.default_rng(3)
+    c = rng.integers(0, 2**32, (4, 16), dtype=np.uint64)
+    k = [int(x) for x in rng.integers(0, 2**32, 2, dtype=np.uint64)]
+    got = oracle.philox4x32_10_arrays(*c, *k)
+    for i in range(16):
+        assert [int(x[i]) for x in got] == oracle.philox4x32_10([int(v) for v in c[:, i]], k)
+
+
+def test_noise_draws_counter_mapping():
+    # element (s, t) -> index e = s*L + t -> output e % 4 of the call with counter e // 4
+    seed = (7 << 32) | 11
+    z = oracle.noise_draws(3, 9, seed, "uniform")
+    for s_, t in ((0, 0), (0, 8), (1, 0), (2, 5)):
+        e = s_ * 9 + t
+        bits = oracle.philox4x32_10([e // 4, 0, 0, 0], [11, 7])[e % 4]
+        assert z[s_, t] == (bits >> 8) / 2.0**24
+    n = oracle.noise_draws(64, 3721, 1, "normal")
+    assert abs(n.mean()) < 5 / np.sqrt(n.size) and abs(n.std() - 1) < 5e-3
+
+
 def test_noise_sigma_nan_rule():
     cube = np.ones((3, 3, 4))
     s, med = oracle.noise_sigma(cube, 10.0)
@@ -102,3 +123,58 @@ def test_noise_statistics(dist):
         # z recovered from float32 values: within rounding of [0, 1)
         assert abs(z.mean() - 0.5) < 5 / np.sqrt(12 * n)
         assert z.min() >= -1e-5 and z.max() < 1 + 1e-5
+
+
+def _apply_noise_rows(rows, L, flux, median, dist, seed):
+    """rubix_apply_noise on a [spaxels, >= L] float32 view (any row stride)."""
+    from rubix_gb300 import _lib, ops
+
+    _lib.call("rubix_apply_noise", ops._ptr(rows), rows.shape[0], L, rows.stride(0),
+              ops._ptr(flux), ops._ptr(median), 20.0, {"normal": 0, "uniform": 1}[dist],
+              seed, ops._stream(rows.device))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dist", ["normal", "uniform"])
+def test_noise_draws_match_counter_mapping(dist):
+    """Every element's draw is the oracle's Philox output for its counter; the float4
+    path (unpadded, aligned), the element path of a misaligned cube and of padded rows
+    give bit-identical cubes."""
+    import torch
+
+    from rubix_gb300 import ops
+
+    rng = np.random.default_rng(4)
+    n_sp, L = 35, 37  # odd L: quads straddle spaxel rows
+    seed = (5 << 32) | 99
+    base = rng.uniform(1.0, 3.0, (n_sp, L)).astype(np.float32)
+    cube = to_dev(base)
+    flux = ops.flux_image(cube)
+    med = ops.noise_median(flux)
+    _apply_noise_rows(cube, L, flux, med, dist, seed)
+    # misaligned start (element path) and padded rows (element path)
+    buf = torch.zeros(n_sp * L + 1, dtype=torch.float32, device=cube.device)
+    mis = buf[1:].view(n_sp, L)
+    mis.copy_(to_dev(base))
+    _apply_noise_rows(mis, L, flux, med, dist, seed)
+    pad = torch.zeros(n_sp, L + 3, dtype=torch.float32, device=cube.device)
+    pad[:, :L] = to_dev(base)
+    _apply_noise_rows(pad, L, flux, med, dist, seed)
+    torch.cuda.synchronize()
+    got = cube.cpu().numpy()
+    assert np.array_equal(got, mis.cpu().numpy())
+    assert np.array_equal(got, pad[:, :L].cpu().numpy())
+    assert not pad[:, L:].any()
+
+    f = flux.cpu().numpy()
+    scale = np.float32(np.sqrt(np.float32(med.item()))) * (np.float32(1) / np.float32(20))
+    sig = (scale / np.sqrt(f)).astype(np.float32)
+    z = oracle.noise_draws(n_sp, L, seed, dist)
+    if dist == "uniform":
+        w = (sig[:, None] * z.astype(np.float32)).astype(np.float32)
+        want = (base.astype(np.float64) + base.astype(np.float64) * w).astype(np.float32)
+        ulps = np.abs(got.view(np.int32).astype(np.int64) - want.view(np.int32))
+        assert ulps.max() <= 1 and (ulps == 0).mean() > 0.99
+    else:
+        zg = (got.astype(np.float64) - base) / (base * sig[:, None].astype(np.float64))
+        np.testing.assert_allclose(zg, z, rtol=0, atol=5e-4)
