@@ -504,6 +504,33 @@ RUBIX_API int rubix_inertia_tensor(const float* positions, int64_t n, int64_t st
 RUBIX_API int rubix_rotate_vectors(const float* in, float* out, int64_t n, int64_t stride_in,
                                    int64_t stride_out, const double* matrix9, void* stream);
 
+/*
+ * rotate_galaxy + filter_particles + spaxel_assignment of one particle component in one
+ * pass (replaces the rotate_vectors / aperture-mask / masked-copy / assignment launches
+ * of rubix/core/rotation.py:66-113, rubix/core/telescope.py:151-199 and
+ * rubix/core/telescope.py:81-126 when the three steps run back to back):
+ *   coords, velocity: [n][3] float32, contiguous;
+ *   matrix9: host row-major 3x3 float64 M, or NULL for no rotation; with M,
+ *     coords_out[i] = coords[i] . M and velocity_out[i] = velocity[i] . M (as
+ *     rubix_rotate_vectors; out may alias in), and the turned coordinates are the ones
+ *     masked and assigned;
+ *   mask_out[i] = 1 inside the inclusive aperture [min(edges), max(edges)]^2 (as
+ *     rubix_aperture_mask); may be NULL when n_fields == 0;
+ *   fields: n_fields (<= 8) float32 per-particle arrays of field_widths[f] values each
+ *     (host arrays of device pointers), copied to fields_out[f] with the particles
+ *     outside set to 0 (filter_particles; out may alias in);
+ *   idx_out[i] = the flat spaxel index of the (turned) coordinates (as
+ *     rubix_spaxel_assign).
+ */
+RUBIX_API int rubix_orient_filter_assign(const float* coords, const float* velocity, int64_t n,
+                                         const double* matrix9, float* coords_out,
+                                         float* velocity_out, const float* edges,
+                                         int32_t n_edges, int32_t n_fields,
+                                         const float* const* fields_in,
+                                         float* const* fields_out,
+                                         const int32_t* field_widths, uint8_t* mask_out,
+                                         int32_t* idx_out, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Observation noise                                                         */
 /* ------------------------------------------------------------------------- */

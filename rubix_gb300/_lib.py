@@ -109,6 +109,9 @@ SIGNATURES = {
     "rubix_inertia_workspace_size": (_sz, []),
     "rubix_inertia_tensor": (_c.c_int, [_vp, _i64, _i64, _vp, _c.c_float, _vp, _vp, _sz, _vp]),
     "rubix_rotate_vectors": (_c.c_int, [_vp, _vp, _i64, _i64, _i64, _vp, _vp]),
+    "rubix_orient_filter_assign": (
+        _c.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp]
+    ),
     "rubix_flux_image": (_c.c_int, [_vp, _i64, _i32, _i64, _vp, _vp]),
     "rubix_noise_median_workspace_size": (_sz, []),
     "rubix_noise_median": (_c.c_int, [_vp, _i64, _vp, _vp, _sz, _vp]),

@@ -93,6 +93,26 @@ def to_device(x, device, dtype=torch.float32) -> torch.Tensor:
     return t.contiguous()
 
 
+_CONSTANTS: dict = {}
+
+
+def device_constant(x, device, dtype=torch.float32) -> torch.Tensor:
+    """A host constant of the configuration (bin edges, wavelength grids, extinction
+    exponents) on the device, uploaded once per (contents, device, dtype).  A copy from
+    pageable host memory waits for the stream's queued work, so steps that uploaded their
+    constants on every call kept the host from running ahead of the GPU.  The tensors
+    are shared: callers must not write to them."""
+    a = np.ascontiguousarray(np.asarray(x))
+    key = (a.dtype.str, a.shape, a.tobytes(), str(torch.device(device)), str(dtype))
+    t = _CONSTANTS.get(key)
+    if t is None:
+        if len(_CONSTANTS) >= 256:
+            _CONSTANTS.clear()
+        t = to_device(a, device, dtype)
+        _CONSTANTS[key] = t
+    return t
+
+
 _VECTOR_FIELDS = ("coords", "velocity")
 
 

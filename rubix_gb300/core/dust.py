@@ -21,7 +21,7 @@ from .. import ops
 from .. import telescope as tel
 from ..logging import get_logger
 from .config import rubix_config
-from .data import RubixData, device_of, flat_particles, to_device
+from .data import RubixData, device_constant, device_of, flat_particles, to_device
 from .ifu import ParticleSpectra, _spectra_tensor
 from .telescope import get_spatial_bin_edges, get_telescope
 
@@ -81,8 +81,8 @@ def apply_spaxel_extinction(config: dict, rubixdata: RubixData, wavelength, n_sp
             f"{dust_host.RV_MODELS}.")
     dev = device_of(config)
     av = star_av(config, rubixdata, n_spaxels, float(np.asarray(spaxel_area)))
-    exponent = to_device(dust_host.extinction_exponent(np.asarray(wavelength), ext_model, Rv),
-                         dev)
+    exponent = device_constant(
+        dust_host.extinction_exponent(np.asarray(wavelength), ext_model, Rv), dev)
     spec = rubixdata.stars.spectra
     if isinstance(spec, ParticleSpectra) and spec.stage == "resampled":
         return dataclasses.replace(spec, dust_av=av, dust_exponent=exponent)

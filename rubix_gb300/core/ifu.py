@@ -24,7 +24,7 @@ from .. import ops
 from .. import telescope as tel
 from ..logging import get_logger
 from .config import rubix_config
-from .data import RubixData, device_of, flat_particles, has_device_axis, to_device
+from .data import RubixData, device_constant, device_of, flat_particles, has_device_axis, to_device
 from .ssp import get_ssp, lookup_method
 from .lsf import EXTEND_FACTOR
 from .telescope import get_telescope
@@ -163,8 +163,8 @@ def get_doppler_shift_and_resampling(config: dict) -> Callable:
     wave_t_np = np.asarray(telescope.wave_seq, dtype=np.float32)
 
     def doppler_shift_and_resampling(rubixdata: RubixData) -> RubixData:
-        wave_z = to_device(wave_z_np, dev)
-        wave_t = to_device(wave_t_np, dev)
+        wave_z = device_constant(wave_z_np, dev)
+        wave_t = device_constant(wave_t_np, dev)
         for name in ("stars", "gas"):
             comp = getattr(rubixdata, name)
             if comp is None or comp.spectra is None:

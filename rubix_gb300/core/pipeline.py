@@ -13,7 +13,7 @@ import time
 from typing import Optional
 
 from ..logging import get_logger
-from ..pipeline import LinearTransformerPipeline
+from ..pipeline import LinearTransformerPipeline, step_names
 from .config import get_config, get_pipeline_config
 from .data import RubixData, get_reshape_data
 from .dust import get_extinction
@@ -24,16 +24,20 @@ from .noise import get_apply_noise
 from .psf import get_convolve_psf
 from .rotation import get_galaxy_rotation
 from .ssp import get_ssp
-from .telescope import get_filter_particles, get_spaxel_assignment, get_telescope
+from .telescope import (FrameHandoff, frame_fusion, get_filter_particles,
+                        get_spaxel_assignment, get_telescope)
 
 
 class RubixPipeline:
     """``fuse_lsf``: when the pipeline runs convolve_lsf after calculate_datacube with
     only convolve_psf between them, apply the LSF in the accumulate kernel's epilogue
-    (the two convolutions commute) instead of in a separate pass over the cube."""
+    (the two convolutions commute) instead of in a separate pass over the cube.
+    ``fuse_frame``: when filter_particles is directly followed by spaxel_assignment
+    (and directly preceded by rotate_galaxy), turn, filter and assign the particles in
+    one pass.  Neither changes the result of the run."""
 
     def __init__(self, user_config, data: Optional[RubixData] = None, *,
-                 fuse_lsf: bool = True):
+                 fuse_lsf: bool = True, fuse_frame: bool = True):
         self.user_config = get_config(user_config)
         self.pipeline_config = get_pipeline_config(self.user_config["pipeline"]["name"])
         self.logger = get_logger(self.user_config.get("logger"))
@@ -44,15 +48,17 @@ class RubixPipeline:
         self.data = data
         self.func = None
         self.fuse_lsf = fuse_lsf
+        self.fuse_frame = fuse_frame
 
-    def _get_pipeline_functions(self, handoff: Optional[LsfHandoff] = None) -> list:
+    def _get_pipeline_functions(self, handoff: Optional[LsfHandoff] = None,
+                                frame: Optional[FrameHandoff] = None) -> list:
         c = self.user_config
         lsf = get_convolve_lsf(c, handoff)
         funcs = [
-            get_galaxy_rotation(c), get_filter_particles(c), get_spaxel_assignment(c),
-            get_calculate_spectra(c), get_reshape_data(c), get_scale_spectrum_by_mass(c),
-            get_doppler_shift_and_resampling(c), get_calculate_datacube(c, handoff),
-            get_convolve_psf(c), lsf, get_apply_noise(c),
+            get_galaxy_rotation(c, frame), get_filter_particles(c, frame),
+            get_spaxel_assignment(c, frame), get_calculate_spectra(c), get_reshape_data(c),
+            get_scale_spectrum_by_mass(c), get_doppler_shift_and_resampling(c),
+            get_calculate_datacube(c, handoff), get_convolve_psf(c), lsf, get_apply_noise(c),
         ]
         # rubix builds calculate_extinction for every pipeline (core/pipeline.py:114);
         # here it is built when the configuration has a dust section
@@ -62,11 +68,11 @@ class RubixPipeline:
 
     def run(self) -> RubixData:
         t0 = time.time()
-        self._pipeline = LinearTransformerPipeline(self.pipeline_config,
-                                                   self._get_pipeline_functions())
-        if self.fuse_lsf and lsf_fusable(self._pipeline._names):
-            self._pipeline = LinearTransformerPipeline(
-                self.pipeline_config, self._get_pipeline_functions(LsfHandoff()))
+        names = step_names(self.pipeline_config)
+        lsf = LsfHandoff() if self.fuse_lsf and lsf_fusable(names) else None
+        frame = frame_fusion(names) if self.fuse_frame else None
+        self._pipeline = LinearTransformerPipeline(
+            self.pipeline_config, self._get_pipeline_functions(lsf, frame))
         self.func = self._pipeline.expression
         out = self.func(self.data)
         import torch

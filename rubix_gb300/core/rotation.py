@@ -37,7 +37,10 @@ def rotation_matrix_from_inertia_tensor(I) -> np.ndarray:
     return v[:, np.argsort(w)]
 
 
-def get_galaxy_rotation(config: dict) -> Callable:
+def get_galaxy_rotation(config: dict, handoff=None) -> Callable:
+    """rubix/core/rotation.py:11-117.  With ``handoff`` (a ``core.telescope.FrameHandoff``
+    whose ``rotation`` is set) the matrix is derived here and the turn itself runs in the
+    spaxel_assignment pass that follows."""
     if "rotation" not in config["galaxy"]:
         raise ValueError("Rotation information not provided in galaxy config")
     logger = get_logger(config.get("logger", None))
@@ -73,6 +76,9 @@ def get_galaxy_rotation(config: dict) -> Callable:
             mass = to_device(comp.mass, dev)
             I = ops.inertia_tensor(coords, mass, hmr).cpu().numpy()
             M = rotation_matrix_from_inertia_tensor(I) @ R_euler
+            if handoff is not None and handoff.rotation:
+                handoff.matrix[particle_type] = (M, coords, vel)
+                continue
             comp.coords = ops.rotate_vectors(coords, M)
             comp.velocity = ops.rotate_vectors(vel, M)
         return rubixdata

@@ -3,7 +3,7 @@
 
 from __future__ import annotations
 
-from typing import Callable
+from typing import Callable, Optional
 
 import numpy as np
 import torch
@@ -11,7 +11,7 @@ import torch
 from .. import ops
 from .. import telescope as tel
 from ..logging import get_logger
-from .data import RubixData, device_of, flat_particles, has_device_axis, to_device
+from .data import RubixData, device_constant, device_of, flat_particles, has_device_axis, to_device
 
 _CUSTOM = {}
 
@@ -44,8 +44,94 @@ def _component(rubixdata: RubixData, name: str):
     return getattr(rubixdata, name)
 
 
-def get_spaxel_assignment(config: dict) -> Callable:
-    """rubix/core/telescope.py:80-126 (square pixels only)."""
+class FrameHandoff:
+    """Links rotate_galaxy, filter_particles and spaxel_assignment of one pipeline run
+    when they run back to back (calc_ifu's order).  rotate_galaxy derives each
+    component's rotation matrix (``matrix``: name -> (M, device coords, device
+    velocity)), filter_particles records which components it filters (``filter``), and
+    spaxel_assignment turns, filters and assigns the particles in one pass
+    (``rubix_orient_filter_assign``) instead of a launch per array."""
+
+    def __init__(self, rotation: bool = True):
+        self.rotation = rotation  # rotate_galaxy defers to spaxel_assignment
+        self.matrix: dict = {}
+        self.filter = None
+
+
+def frame_fusion(step_names):
+    """A FrameHandoff for a run whose filter_particles is directly followed by
+    spaxel_assignment (with rotate_galaxy directly before them, the rotation joins the
+    pass as well); None otherwise."""
+    names = list(step_names)
+    for i in range(len(names) - 1):
+        if names[i] == "filter_particles" and names[i + 1] == "spaxel_assignment":
+            return FrameHandoff(rotation=i > 0 and names[i - 1] == "rotate_galaxy")
+    return None
+
+
+def _filter_targets(comp, name: str):
+    """The arrays filter_particles zeroes outside the aperture: every per-particle array
+    but coords, velocity (and the gas metals), as (attr, value) pairs."""
+    skip = ("coords", "velocity") + (("metals",) if name == "gas" else ())
+    out = []
+    for attr, val in list(vars(comp).items()):
+        if attr in skip or attr in ("mask", "spatial_bin_edges") or val is None:
+            continue
+        if not isinstance(val, (np.ndarray, torch.Tensor)) or np.ndim(val) == 0:
+            continue
+        out.append((attr, val))
+    return out
+
+
+def _masked_copy(val, mask, dev):
+    t = to_device(val, dev, torch.float32 if _is_float(val) else None).clone()
+    if t.dtype == torch.float32:
+        return ops.mask_zero_(t, mask)
+    return torch.where(_expand(mask, t), t, torch.zeros((), dtype=t.dtype, device=dev))
+
+
+def _fused_frame(rubixdata: RubixData, handoff: FrameHandoff, edges, dev) -> None:
+    """The deferred rotation and filter of each component with the assignment, in one
+    rubix_orient_filter_assign launch per component."""
+    for name in ("stars", "gas"):
+        comp = getattr(rubixdata, name)
+        if comp is None or comp.coords is None:
+            continue
+        pend = handoff.matrix.pop(name, None)
+        if pend is not None:
+            M, coords, vel = pend
+        else:
+            M, coords, vel = None, to_device(comp.coords, dev), None
+        filt = handoff.filter is not None and name in handoff.filter
+        fields, attrs, others = [], [], []
+        if filt:
+            for attr, val in _filter_targets(comp, name):
+                if _is_float(val) and len(fields) < 8:
+                    fields.append(to_device(val, dev, torch.float32))
+                    attrs.append(attr)
+                else:
+                    others.append((attr, val))
+        co, vo, outs, mask, idx = ops.orient_filter_assign(
+            coords.reshape(-1, 3), None if vel is None else vel.reshape(-1, 3), M, edges,
+            fields, mask=filt)
+        axis = has_device_axis(comp.coords, True)
+        if M is not None:
+            comp.coords = co.reshape(coords.shape)
+            comp.velocity = vo.reshape(vel.shape)
+        if filt:
+            for attr, o in zip(attrs, outs):
+                setattr(comp, attr, o)
+            for attr, val in others:
+                setattr(comp, attr, _masked_copy(val, mask, dev))
+            comp.mask = mask.bool().unsqueeze(0) if axis else mask.bool()
+        comp.pixel_assignment = idx.unsqueeze(0) if axis else idx
+        comp.spatial_bin_edges = edges
+    handoff.filter = None
+
+
+def get_spaxel_assignment(config: dict, handoff: Optional[FrameHandoff] = None) -> Callable:
+    """rubix/core/telescope.py:80-126 (square pixels only).  With ``handoff`` the
+    rotation and filter deferred by the two steps before run in the same launch."""
     logger = get_logger(config.get("logger", None))
     telescope = get_telescope(config)
     if telescope.pixel_type not in ["square"]:
@@ -55,7 +141,10 @@ def get_spaxel_assignment(config: dict) -> Callable:
 
     def spaxel_assignment(rubixdata: RubixData) -> RubixData:
         logger.info("Assigning particles to spaxels...")
-        edges = to_device(edges_np, dev)
+        edges = device_constant(edges_np, dev)
+        if handoff is not None and (handoff.filter is not None or handoff.matrix):
+            _fused_frame(rubixdata, handoff, edges, dev)
+            return rubixdata
         for comp in (rubixdata.stars, rubixdata.gas):
             if comp is None or comp.coords is None:
                 continue
@@ -68,9 +157,10 @@ def get_spaxel_assignment(config: dict) -> Callable:
     return spaxel_assignment
 
 
-def get_filter_particles(config: dict) -> Callable:
+def get_filter_particles(config: dict, handoff: Optional[FrameHandoff] = None) -> Callable:
     """rubix/core/telescope.py:129-201: particles outside the aperture get every
-    non-coordinate, non-velocity field set to 0 and ``mask`` records who is inside."""
+    non-coordinate, non-velocity field set to 0 and ``mask`` records who is inside.
+    With ``handoff`` the filter is left to the spaxel_assignment that follows."""
     logger = get_logger(config.get("logger", None))
     edges_np = get_spatial_bin_edges(config)
     dev = device_of(config)
@@ -78,25 +168,18 @@ def get_filter_particles(config: dict) -> Callable:
 
     def filter_particles(rubixdata: RubixData) -> RubixData:
         logger.info("Filtering particles outside the aperture...")
-        edges = to_device(edges_np, dev)
+        if handoff is not None:
+            handoff.filter = tuple(types)
+            return rubixdata
+        edges = device_constant(edges_np, dev)
         for name in ("stars", "gas"):
             comp = getattr(rubixdata, name)
             if name not in types or comp is None or comp.coords is None:
                 continue
             coords = flat_particles(comp.coords, dev, width=3)
             mask = ops.aperture_mask(coords, edges)
-            skip = ("coords", "velocity") + (("metals",) if name == "gas" else ())
-            for attr, val in list(vars(comp).items()):
-                if attr in skip or attr in ("mask", "spatial_bin_edges") or val is None:
-                    continue
-                if not isinstance(val, (np.ndarray, torch.Tensor)) or np.ndim(val) == 0:
-                    continue
-                t = to_device(val, dev, torch.float32 if _is_float(val) else None).clone()
-                if t.dtype == torch.float32:
-                    ops.mask_zero_(t, mask)
-                else:
-                    t = torch.where(_expand(mask, t), t, torch.zeros((), dtype=t.dtype, device=dev))
-                setattr(comp, attr, t)
+            for attr, val in _filter_targets(comp, name):
+                setattr(comp, attr, _masked_copy(val, mask, dev))
             comp.mask = mask.bool().unsqueeze(0) if has_device_axis(comp.coords, True) else mask.bool()
         return rubixdata
 

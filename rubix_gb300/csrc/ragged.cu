@@ -5,19 +5,10 @@
 //     persistent launch renders every galaxy of the batch;
 //   * per-galaxy dot products (the PSF-width gradients of a batch).
 #include "common.cuh"
+#include "particle_frame.cuh"
 
 namespace rubix {
 namespace {
-
-__device__ __forceinline__ int count_le_edges(const float* e, int n, float x) {
-  if (x != x) return n;
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (e[mid] <= x) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
 
 // Per particle: galaxy by binary search on poff; ix, iy = clip(digitize - 1) on the
 // galaxy's edges (rubix/telescope/utils.py:138-151); kept when inside the inclusive
@@ -40,15 +31,9 @@ __global__ void ragged_assign_kernel(const float* __restrict__ coords, long long
     const int g = lo;
     const float* e = edges + eoff[g];
     const int ne = eoff[g + 1] - eoff[g];
-    const int nb = ne - 1;
     const float x = coords[i * stride], y = coords[i * stride + 1];
-    int ix = count_le_edges(e, ne, x) - 1;
-    int iy = count_le_edges(e, ne, y) - 1;
-    ix = min(max(ix, 0), nb - 1);
-    iy = min(max(iy, 0), nb - 1);
-    const int local = ix + nb * iy;
-    const float elo = e[0], ehi = e[ne - 1];
-    const bool inside = x >= elo && x <= ehi && y >= elo && y <= ehi;
+    const int local = spaxel_index(e, ne, x, y);
+    const bool inside = inside_aperture(x, y, e[0], e[ne - 1]);
     const int S = sbin[g];
     const bool keep = inside && local < S * S;
     idx_out[i] = keep ? (int)(seg_base[g] + local) : 0;

@@ -8,6 +8,7 @@
 // per-thread partials, block partials, then one block adding the block partials in
 // index order (deterministic).
 #include "common.cuh"
+#include "particle_frame.cuh"
 
 namespace rubix {
 namespace {
@@ -95,18 +96,12 @@ __global__ void __launch_bounds__(kInVals * 32) inertia_finish_kernel(
   out[8] = v[2];
 }
 
-struct Mat3 {
-  double m[9];
-};
-
 __global__ void rotate_kernel(const float* __restrict__ in, float* __restrict__ out,
                               long long n, long long stride_in, long long stride_out, Mat3 M) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const double x = in[i * stride_in], y = in[i * stride_in + 1], z = in[i * stride_in + 2];
-    out[i * stride_out] = (float)(x * M.m[0] + y * M.m[3] + z * M.m[6]);
-    out[i * stride_out + 1] = (float)(x * M.m[1] + y * M.m[4] + z * M.m[7]);
-    out[i * stride_out + 2] = (float)(x * M.m[2] + y * M.m[5] + z * M.m[8]);
+    rotate_row(in[i * stride_in], in[i * stride_in + 1], in[i * stride_in + 2], M,
+               out[i * stride_out], out[i * stride_out + 1], out[i * stride_out + 2]);
   }
 }
 

@@ -6,6 +6,7 @@
 // which each tile ranks its keys with warp-level match/popc and per-warp digit
 // counters.  No float atomics anywhere; the result is deterministic.
 #include "common.cuh"
+#include "particle_frame.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
 
@@ -13,18 +14,6 @@ namespace rubix {
 namespace {
 
 constexpr int kMaxSmemEdges = 8192;
-
-// Number of edges <= x (searchsorted side='right'); NaN counts as above all edges,
-// matching the NaN-last comparator of jnp.digitize.
-__device__ __forceinline__ int count_le(const float* e, int n, float x) {
-  if (x != x) return n;
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (e[mid] <= x) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
 
 __global__ void aperture_mask_kernel(const float* __restrict__ coords, long long n,
                                      long long stride, const float* __restrict__ edges,
@@ -43,8 +32,7 @@ __global__ void aperture_mask_kernel(const float* __restrict__ coords, long long
   const float lo = s_lo, hi = s_hi;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    float x = coords[i * stride], y = coords[i * stride + 1];
-    mask[i] = (x >= lo && x <= hi && y >= lo && y <= hi) ? 1 : 0;
+    mask[i] = inside_aperture(coords[i * stride], coords[i * stride + 1], lo, hi) ? 1 : 0;
   }
 }
 
@@ -58,14 +46,68 @@ __global__ void spaxel_assign_kernel(const float* __restrict__ coords, long long
     __syncthreads();
   }
   const float* e = in_smem ? s_edges : edges;
-  const int nb = n_edges - 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    idx_out[i] = spaxel_index(e, n_edges, coords[i * stride], coords[i * stride + 1]);
+}
+
+constexpr int kMaxFrameFields = 8;
+
+// Per-particle float32 fields copied with the particles outside the aperture set to 0.
+struct FrameFields {
+  const float* in[kMaxFrameFields];
+  float* out[kMaxFrameFields];
+  int width[kMaxFrameFields];
+  int n;
+};
+
+// rotate_galaxy + filter_particles + spaxel_assignment in one pass over the particles:
+// coordinates and velocities turned by M (when rotate), the aperture mask of the turned
+// coordinates, the masked copies of the fields, and the flat spaxel index.  The same
+// per-particle arithmetic as rotate_kernel, aperture_mask_kernel and spaxel_assign_kernel.
+__global__ void frame_assign_kernel(const float* coords, const float* velocity, long long n,
+                                    int rotate, Mat3 M, float* coords_out, float* velocity_out,
+                                    const float* __restrict__ edges, int n_edges, FrameFields F,
+                                    unsigned char* __restrict__ mask_out,
+                                    int* __restrict__ idx_out) {
+  extern __shared__ float s_edges[];
+  __shared__ float s_lo, s_hi;
+  const bool in_smem = n_edges <= kMaxSmemEdges;
+  if (in_smem)
+    for (int i = threadIdx.x; i < n_edges; i += blockDim.x) s_edges[i] = edges[i];
+  if (threadIdx.x == 0) {
+    float lo = edges[0], hi = edges[0];
+    for (int i = 1; i < n_edges; ++i) {
+      lo = fminf(lo, edges[i]);
+      hi = fmaxf(hi, edges[i]);
+    }
+    s_lo = lo;
+    s_hi = hi;
+  }
+  __syncthreads();
+  const float* e = in_smem ? s_edges : edges;
+  const float lo = s_lo, hi = s_hi;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    int ix = count_le(e, n_edges, coords[i * stride]) - 1;
-    int iy = count_le(e, n_edges, coords[i * stride + 1]) - 1;
-    ix = min(max(ix, 0), nb - 1);
-    iy = min(max(iy, 0), nb - 1);
-    idx_out[i] = ix + nb * iy;
+    float x = coords[3 * i], y = coords[3 * i + 1], z = coords[3 * i + 2];
+    if (rotate) {
+      rotate_row(x, y, z, M, x, y, z);
+      coords_out[3 * i] = x;
+      coords_out[3 * i + 1] = y;
+      coords_out[3 * i + 2] = z;
+      float vx, vy, vz;
+      rotate_row(velocity[3 * i], velocity[3 * i + 1], velocity[3 * i + 2], M, vx, vy, vz);
+      velocity_out[3 * i] = vx;
+      velocity_out[3 * i + 1] = vy;
+      velocity_out[3 * i + 2] = vz;
+    }
+    const bool inside = inside_aperture(x, y, lo, hi);
+    if (mask_out) mask_out[i] = inside ? 1 : 0;
+    for (int f = 0; f < F.n; ++f) {
+      const int w = F.width[f];
+      for (int k = 0; k < w; ++k) F.out[f][i * w + k] = inside ? F.in[f][i * w + k] : 0.f;
+    }
+    idx_out[i] = spaxel_index(e, n_edges, x, y);
   }
 }
 
@@ -147,6 +189,59 @@ extern "C" int rubix_spaxel_assign(const float* coords, int64_t n, int64_t coord
   spaxel_assign_kernel<<<grid_for(n, 256), 256, smem, st>>>(coords, n, coord_stride, edges,
                                                              n_edges, idx_out);
   RUBIX_LAUNCH_CHECK("spaxel_assign_kernel");
+  return RUBIX_OK;
+}
+
+extern "C" int rubix_orient_filter_assign(const float* coords, const float* velocity,
+                                          int64_t n, const double* matrix9, float* coords_out,
+                                          float* velocity_out, const float* edges,
+                                          int32_t n_edges, int32_t n_fields,
+                                          const float* const* fields_in,
+                                          float* const* fields_out,
+                                          const int32_t* field_widths, uint8_t* mask_out,
+                                          int32_t* idx_out, void* stream) {
+  RUBIX_REQUIRE(n >= 0, RUBIX_E_INVALID, "rubix_orient_filter_assign: n < 0");
+  RUBIX_REQUIRE(n_edges >= 2, RUBIX_E_SHAPE,
+                "rubix_orient_filter_assign: need at least two edges");
+  RUBIX_REQUIRE((long long)(n_edges - 1) * (n_edges - 1) < (1LL << 31), RUBIX_E_SHAPE,
+                "rubix_orient_filter_assign: (n_edges-1)^2 overflows int32");
+  RUBIX_REQUIRE(n_fields >= 0 && n_fields <= kMaxFrameFields, RUBIX_E_INVALID,
+                "rubix_orient_filter_assign: n_fields must be in [0, %d]", kMaxFrameFields);
+  RUBIX_REQUIRE(n_fields == 0 || (fields_in && fields_out && field_widths), RUBIX_E_INVALID,
+                "rubix_orient_filter_assign: null field arrays");
+  RUBIX_REQUIRE(n_fields == 0 || mask_out, RUBIX_E_INVALID,
+                "rubix_orient_filter_assign: filtered fields need mask_out");
+  FrameFields F;
+  F.n = n_fields;
+  for (int f = 0; f < kMaxFrameFields; ++f) {
+    F.in[f] = nullptr;
+    F.out[f] = nullptr;
+    F.width[f] = 0;
+  }
+  for (int f = 0; f < n_fields; ++f) {
+    RUBIX_REQUIRE(field_widths[f] >= 1, RUBIX_E_SHAPE,
+                  "rubix_orient_filter_assign: field %d has width < 1", f);
+    RUBIX_REQUIRE(n == 0 || (fields_in[f] && fields_out[f]), RUBIX_E_INVALID,
+                  "rubix_orient_filter_assign: field %d has a null pointer", f);
+    F.in[f] = fields_in[f];
+    F.out[f] = fields_out[f];
+    F.width[f] = field_widths[f];
+  }
+  if (n == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(coords && edges && idx_out, RUBIX_E_INVALID,
+                "rubix_orient_filter_assign: null pointer");
+  Mat3 M;
+  for (int i = 0; i < 9; ++i) M.m[i] = matrix9 ? matrix9[i] : (i % 4 == 0 ? 1.0 : 0.0);
+  if (matrix9)
+    RUBIX_REQUIRE(velocity && coords_out && velocity_out, RUBIX_E_INVALID,
+                  "rubix_orient_filter_assign: a rotation needs velocity, coords_out and "
+                  "velocity_out");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  size_t smem = n_edges <= kMaxSmemEdges ? (size_t)n_edges * sizeof(float) : 0;
+  frame_assign_kernel<<<grid_for(n, 256), 256, smem, st>>>(
+      coords, velocity, n, matrix9 ? 1 : 0, M, coords_out, velocity_out, edges, n_edges, F,
+      mask_out, idx_out);
+  RUBIX_LAUNCH_CHECK("frame_assign_kernel");
   return RUBIX_OK;
 }
 

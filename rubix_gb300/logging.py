@@ -9,8 +9,9 @@ def get_logger(config=None) -> logging.Logger:
     """The "rubix_gb300" logger; ``config`` may set ``log_level`` and ``format``."""
     logger = logging.getLogger("rubix_gb300")
     if config:
-        level = config.get("log_level", "INFO")
-        logger.setLevel(getattr(logging, str(level).upper(), logging.INFO))
+        level = getattr(logging, str(config.get("log_level", "INFO")).upper(), logging.INFO)
+        if logger.level != level:  # setLevel clears every logger's cache
+            logger.setLevel(level)
         fmt = config.get("format")
         if fmt and not logger.handlers:
             h = logging.StreamHandler()

@@ -294,6 +294,56 @@ def rotate_vectors(x: torch.Tensor, matrix, out=None) -> torch.Tensor:
     return out.reshape(x.shape)
 
 
+def orient_filter_assign(coords, velocity, matrix, edges, fields=(), mask=True,
+                         out_coords=None, out_velocity=None):
+    """rotate_galaxy + filter_particles + spaxel_assignment in one launch.
+
+    coords, velocity: [n, 3] float32 (velocity used only with ``matrix``); matrix: 3x3
+    (host) or None; fields: float32 tensors with n rows, copied with the particles
+    outside the aperture set to 0.  Returns (coords_out, velocity_out, fields_out, mask
+    uint8 or None, idx int32); without ``matrix`` coords_out / velocity_out are None."""
+    import ctypes
+
+    coords = _contig("coords", coords, torch.float32)
+    n = coords.shape[0]
+    if coords.dim() != 2 or coords.shape[1] != 3:
+        raise ValueError(f"coords must be (n, 3), got {tuple(coords.shape)}")
+    edges = _contig("edges", edges, torch.float32)
+    dev = coords.device
+    m = None
+    if matrix is not None:
+        m = np.ascontiguousarray(np.asarray(matrix, dtype=np.float64).reshape(3, 3))
+        velocity = _contig("velocity", velocity, torch.float32)
+        if tuple(velocity.shape) != (n, 3):
+            raise ValueError("velocity must be (n, 3) like coords")
+        out_coords = torch.empty_like(coords) if out_coords is None else out_coords
+        out_velocity = torch.empty_like(velocity) if out_velocity is None else out_velocity
+    fields = [_contig("field", f, torch.float32) for f in fields]
+    if len(fields) > 8:
+        raise ValueError("at most 8 fields per launch")
+    widths = []
+    for f in fields:
+        w = f.numel() // max(n, 1) if n else 1
+        if n and f.numel() != n * w:
+            raise ValueError("every field needs one row per particle")
+        widths.append(max(w, 1))
+    outs = [torch.empty_like(f) for f in fields]
+    mask_t = torch.empty(n, dtype=torch.uint8, device=dev) if (mask or fields) else None
+    idx = torch.empty(n, dtype=torch.int32, device=dev)
+    k = len(fields)
+    fin = (ctypes.c_void_p * max(k, 1))(*[f.data_ptr() for f in fields])
+    fout = (ctypes.c_void_p * max(k, 1))(*[o.data_ptr() for o in outs])
+    fw = (ctypes.c_int32 * max(k, 1))(*widths)
+    _lib.call("rubix_orient_filter_assign", _ptr(coords), _ptr(velocity) if m is not None else None,
+              n, None if m is None else m.ctypes.data, _ptr(out_coords) if m is not None else None,
+              _ptr(out_velocity) if m is not None else None, _ptr(edges), edges.numel(), k,
+              ctypes.addressof(fin), ctypes.addressof(fout), ctypes.addressof(fw),
+              _ptr(mask_t) if mask_t is not None else None, _ptr(idx), _stream(dev))
+    _count(1 if n > 0 else 0)
+    return (out_coords if m is not None else None, out_velocity if m is not None else None,
+            outs, mask_t, idx)
+
+
 def flux_image(cube: torch.Tensor) -> torch.Tensor:
     """[..., L] -> [...] float32: sum over the last axis (the flux image of a cube)."""
     _check_cuda("cube", cube, torch.float32)

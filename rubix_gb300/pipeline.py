@@ -22,6 +22,21 @@ def bound_transformer(*args, **kwargs):
     return wrap
 
 
+def step_names(cfg: dict) -> List[str]:
+    """The transformer names of a linear pipeline config in run order ([] when the
+    config is not a well-formed chain; ``LinearTransformerPipeline`` reports why)."""
+    try:
+        nodes = cfg["Transformers"]
+        key = next(k for k, n in nodes.items() if n["depends_on"] is None)
+        names = []
+        while key is not None and len(names) <= len(nodes):
+            names.append(nodes[key]["name"])
+            key = next((k for k, n in nodes.items() if n["depends_on"] == key), None)
+        return names
+    except (KeyError, TypeError, AttributeError, StopIteration):
+        return []
+
+
 class LinearTransformerPipeline:
     """Steps registered by ``__name__`` and chained by the ``depends_on`` fields of the
     pipeline config (one start node, no branching)."""

@@ -177,3 +177,17 @@ def test_lsf_fusable_order():
     assert not lsf_fusable(["calculate_datacube", "apply_noise", "convolve_lsf"])
     assert not lsf_fusable(["convolve_lsf", "calculate_datacube"])
     assert not lsf_fusable(["calculate_datacube", "convolve_psf"])
+
+
+def test_frame_fusion_order():
+    from rubix_gb300.core.telescope import frame_fusion
+
+    h = frame_fusion(["rotate_galaxy", "filter_particles", "spaxel_assignment", "x"])
+    assert h is not None and h.rotation
+    h = frame_fusion(["filter_particles", "spaxel_assignment"])
+    assert h is not None and not h.rotation
+    # rotation not directly before the filter: only filter + assignment are joined
+    h = frame_fusion(["rotate_galaxy", "x", "filter_particles", "spaxel_assignment"])
+    assert h is not None and not h.rotation
+    assert frame_fusion(["spaxel_assignment", "filter_particles"]) is None
+    assert frame_fusion(["filter_particles", "x", "spaxel_assignment"]) is None
