@@ -54,6 +54,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the fwd+bwd, plain-GPU-path and ragged-batch measurements")
+    ap.add_argument("--extras", default=None, metavar="NAMES",
+                    help="comma-separated subset of the extra measurements (fwd_bwd, "
+                         "plain_gpu, plain_gpu_fwd_bwd, dusty, fits_layout, noise, "
+                         "pipeline_api, ragged); default all")
     ap.add_argument("--ssp-wave", type=int, default=None, metavar="N",
                     help="synthetic SSP grid with N wavelengths (e.g. 5994, FSPS-sized)")
     ap.add_argument("--dust", type=int, default=0, metavar="N_GAS",
@@ -459,6 +463,28 @@ def pipeline_bench(dev, w, steps, warmup, flush):
                     "unchanged in float32)"}
 
 
+def noise_bench(dev, cube, steps, warmup, flush):
+    """apply_noise (S/N 20, normal draws) on a copy of the final cube: the flux image,
+    the median select and the noise pass; the noise kernel's algorithmic bytes are 2 C
+    (read + write of the cube)."""
+    from rubix_gb300 import ops
+
+    work = cube.clone()
+    flux = ops.flux_image(work)
+    med = ops.noise_median(flux)
+    kernel_ms = _time_steps(lambda: ops.apply_noise_(work, 20.0, "normal", 1, flux=flux,
+                                                     median=med), steps, warmup, flush)
+    step_ms = _time_steps(lambda: ops.apply_noise_(work, 20.0, "normal", 1), steps, warmup,
+                          flush)
+    nbytes = 2 * cube.numel() * 4
+    peak, kind = hbm_peak()
+    return {"kernel": "rubix_apply_noise", "ms": kernel_ms,
+            "ms_with_flux_image_and_median": step_ms,
+            "achieved_gbs": nbytes / (kernel_ms * 1e-3) / 1e9, "peak_gbs": peak,
+            "frac": nbytes / (kernel_ms * 1e-3) / 1e9 / peak, "peak_source": kind,
+            "bytes": nbytes}
+
+
 def fits_bench(dev, cube, steps, warmup, flush):
     """FITS layout of the final cube (transpose to [lambda][x][y] + big-endian) on the
     GPU: algorithmic bytes 2 C per launch (read + write), against the HBM peak."""
@@ -827,8 +853,11 @@ def main():
                 ("plain_gpu_fwd_bwd", lambda: plain_fwd_bwd_bench(dev, args.steps, 1)),
                 ("dusty", lambda: dusty_bench(dev, w, d_in, args.steps, 3, flush)),
                 ("fits_layout", lambda: fits_bench(dev, ours_final, args.steps, 3, flush)),
+                ("noise", lambda: noise_bench(dev, ours_final, args.steps, 3, flush)),
                 ("pipeline_api", lambda: pipeline_bench(dev, w, min(args.steps, 5), 3, flush)),
                 ("ragged", lambda: ragged_bench(dev, 3, 2))):
+            if args.extras is not None and name not in args.extras.split(","):
+                continue
             try:
                 extras[name] = fn()
             except Exception as exc:  # report and keep the main line

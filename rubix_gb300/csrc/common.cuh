@@ -63,4 +63,26 @@ int sm_count();  // cached multiprocessor count of the current device
 constexpr double kSpeedOfLight = 299792.458;  // km/s, rubix_config.yml:8
 constexpr float kFltMax = 3.402823466e+38f;
 
+#ifdef __CUDACC__
+// exp(v / c) rounded once to float32: the Doppler factor of rubix's
+// velocity_doppler_shift (spectra/ifu.py:190).  In float64 by the Taylor series of exp
+// (degree 8, Horner form) for |v| <= 10^4 km/s, where the truncated terms are below
+// 2e-18 of the sum; exp() beyond.  Eight FMAs instead of a general float64 exp keeps
+// the per-particle setup off the slow float64 pipe.
+__device__ __forceinline__ float doppler_factor(float v) {
+  const double x = (double)v * (1.0 / kSpeedOfLight);
+  if (!(fabs(x) <= 1.0e4 / kSpeedOfLight)) return (float)exp(x);
+  double p = 1.0 / 40320.0;
+  p = fma(p, x, 1.0 / 5040.0);
+  p = fma(p, x, 1.0 / 720.0);
+  p = fma(p, x, 1.0 / 120.0);
+  p = fma(p, x, 1.0 / 24.0);
+  p = fma(p, x, 1.0 / 6.0);
+  p = fma(p, x, 0.5);
+  p = fma(p, x, 1.0);
+  p = fma(p, x, 1.0);
+  return (float)p;
+}
+#endif
+
 }  // namespace rubix

@@ -36,9 +36,10 @@ struct CubeCtrl {
   int error;               // 1: a TMA wait timed out
   unsigned dz_min_bits;    // min SSP spacing near the telescope range (float bits)
   unsigned dt_max_bits;    // max telescope bin width (float bits)
-  int pad0;
+  float bmax;              // |B| limit: (vmax / c) / h
   double lnq0;             // log of the lowest wavelength covered by bucket 0
   double h;                // bucket width in log wavelength
+  double inv_h;            // 1 / h
 };
 
 struct ParticleRec {  // 48 bytes, three vector loads
@@ -93,6 +94,8 @@ __global__ void cube_setup_kernel(const float* __restrict__ wave_z, int n_wave,
     ctrl->error = 0;
     ctrl->lnq0 = lnq0;
     ctrl->h = h;
+    ctrl->inv_h = 1.0 / h;
+    ctrl->bmax = (float)(kVmaxKms / kSpeedOfLight / h);
   }
   for (int t = gtid; t < n_t; t += gsz) {
     At[t] = (float)((log((double)wave_t[t]) - lnq0) / h);
@@ -149,27 +152,39 @@ __global__ void cube_corner_table_kernel(const float* __restrict__ flux, int nZ,
 // is alpha * sum_c w_c (prefix[c][kb] - prefix[c][ka-1]): the float32 rounding of
 // lambda'_k = fl32(lambda_z,k * alpha) enters that sum only through telescoping
 // differences, ~1e-7 relative.
-__global__ void cube_prefix_kernel(const float* __restrict__ flux, int rows, int nW,
-                                   const float* __restrict__ wave_z, double* __restrict__ prefix) {
-  // One warp per SSP row: 32 entries at a time, warp-shuffle inclusive scan plus carry.
-  const int lane = threadIdx.x & 31;
-  const int n_warps = (gridDim.x * blockDim.x) >> 5;
-  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += n_warps) {
+constexpr int kPrefixThreads = 128;
+
+// Per SSP row r: prefix[r][k] = sum_{j=1..k} F[r][j] (lambda_z[j] - lambda_z[j-1]) in
+// float64.  One block per row: each thread sums a run of consecutive entries, a block
+// scan of the run totals gives each run's offset, and the run is written out.
+__global__ void __launch_bounds__(kPrefixThreads) cube_prefix_kernel(
+    const float* __restrict__ flux, int rows, int nW, const float* __restrict__ wave_z,
+    double* __restrict__ prefix) {
+  __shared__ double s_warp[kPrefixThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int per = (nW + kPrefixThreads - 1) / kPrefixThreads;
+  const int k0 = threadIdx.x * per;
+  const int k1 = min(k0 + per, nW);
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
     const float* f = flux + (long long)r * nW;
     double* o = prefix + (long long)r * nW;
-    double carry = 0.0;
-    for (int base = 0; base < nW; base += 32) {
-      const int k = base + lane;
-      double x = (k >= 1 && k < nW) ? (double)f[k] * (double)(wave_z[k] - wave_z[k - 1]) : 0.0;
+    double sum = 0.0;
+    for (int k = max(k0, 1); k < k1; ++k) sum += (double)f[k] * (double)(wave_z[k] - wave_z[k - 1]);
+    double x = sum;  // inclusive scan over the block's runs
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const double y = __shfl_up_sync(0xffffffffu, x, d);
-        if (lane >= d) x += y;
-      }
-      x += carry;
-      if (k < nW) o[k] = x;
-      carry = __shfl_sync(0xffffffffu, x, 31);
+    for (int d = 1; d < 32; d <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
     }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    double run = x - sum;
+    for (int w = 0; w < warp; ++w) run += s_warp[w];
+    for (int k = k0; k < k1; ++k) {
+      if (k >= 1) run += (double)f[k] * (double)(wave_z[k] - wave_z[k - 1]);
+      o[k] = run;
+    }
+    __syncthreads();  // s_warp is reused by the next row
   }
 }
 
@@ -184,13 +199,11 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
                                    const double* __restrict__ prefix,
                                    const CubeCtrl* __restrict__ ctrl,
                                    ParticleRec* __restrict__ rec, int with_grad,
-                                   const float* __restrict__ av) {
+                                   const float* __restrict__ av, float alo, float ahi) {
   const long long n_valid = seg_off[n_seg];
   const float t_lo = wave_t[0], t_hi = wave_t[n_t - 1];
-  const double h = ctrl->h;
-  const double vmc = kVmaxKms / kSpeedOfLight;
-  const float bmax = (float)(vmc / h);
-  const float alo = (float)exp(-vmc), ahi = (float)exp(vmc);
+  const double inv_h = ctrl->inv_h;
+  const float bmax = ctrl->bmax;
   // lambda' spacing >= alpha*dz minus two float32 roundings of lambda' (|lambda'| < 2^14)
   const float dz = __uint_as_float(ctrl->dz_min_bits), dt = __uint_as_float(ctrl->dt_max_bits);
   const bool coarse_ok = dz * alo - 4.0e-3f > dt;
@@ -207,9 +220,9 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
     const float ta = dag == 0.f ? 0.f : (A - ag[ia - 1]) / dag;
     const bool outside = (Z < zg[0]) || (Z > zg[nZ - 1]) || (A < ag[0]) || (A > ag[nA - 1]);
     const int cell = outside ? -1 : (iz - 1) * (nA - 1) + (ia - 1);
-    const double vc = (double)v / kSpeedOfLight;
-    const float alpha = (float)exp(vc);
-    float B = (float)(vc / h);
+    const float alpha = doppler_factor(v);
+    // B only seeds the bracket search (first_bracket corrects it exactly)
+    float B = (float)((double)v * (1.0 / kSpeedOfLight) * inv_h);
     B = fminf(fmaxf(B, -bmax), bmax);
     const int ks = count_le_scaled(wave_z, n_wave, alpha, t_lo) - 1;
     const int ke_raw = count_le_scaled(wave_z, n_wave, alpha, t_hi) - 1;
@@ -217,7 +230,8 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
     ke = max(ke, ks);  // keeps the shared-memory row non-empty for any input grid
     const bool coarse = coarse_ok && alpha >= alo && alpha <= ahi;
     // In-range flux sum T: entries ka..kb with t_lo <= lambda'_k <= t_hi, k >= 1.
-    double T = 0.0, TZ = 0.0, TA = 0.0;
+    float T = 0.f;
+    double TZ = 0.0, TA = 0.0;
     if (cell >= 0) {
       int ka = (ks >= 0 && __fmul_rn(wave_z[ks], alpha) >= t_lo) ? ks : ks + 1;
       ka = max(ka, 1);
@@ -225,15 +239,17 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
       if (ka <= kb) {
         const long long r00 = (long long)(iz - 1) * nA + (ia - 1);
         const long long rr[4] = {r00, r00 + nA, r00 + 1, r00 + nA + 1};  // 00, 10, 01, 11
-        const double w[4] = {(1.0 - tz) * (1.0 - ta), (double)tz * (1.0 - ta),
-                             (1.0 - tz) * (double)ta, (double)tz * ta};
+        // float64 differences of the float64 prefix sums, mixed in float32 (rubix's
+        // sum is float32 throughout)
+        const float w[4] = {(1.f - tz) * (1.f - ta), tz * (1.f - ta), (1.f - tz) * ta,
+                            tz * ta};
         double d[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           d[c] = prefix[rr[c] * n_wave + kb] - prefix[rr[c] * n_wave + ka - 1];
-          T += w[c] * d[c];
+          T = fmaf(w[c], (float)d[c], T);
         }
-        T *= (double)alpha;
+        T *= alpha;
         if (with_grad) {
           // dT/dZ and dT/d(age): the bilinear weights' derivatives, same sums
           const double iz_w = dzg == 0.f ? 0.0 : 1.0 / (double)dzg;
@@ -248,7 +264,7 @@ __global__ void cube_gather_kernel(const float* __restrict__ mass, const float* 
     ParticleRec r;
     r.a = make_float4(m, alpha, B, tz);
     r.b = make_int4(cell, ks, ke | (coarse ? 0 : kGenericFlag), __float_as_int(ta));
-    r.c = make_float4((float)T, (float)TZ, (float)TA, av ? av[i] : 0.f);
+    r.c = make_float4(T, (float)TZ, (float)TA, av ? av[i] : 0.f);
     rec[j] = r;
   }
 }
@@ -375,8 +391,9 @@ inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, const CubeTun
                                                 L.ct);
     RUBIX_LAUNCH_CHECK("cube_corner_table_kernel");
     const int rows = in.n_met * in.n_age;
-    cube_prefix_kernel<<<div_up(rows, 8), 256, 0, st>>>(in.ssp_flux, rows, in.n_wave,
-                                                        in.ssp_wave_z, L.prefix);
+    const int pg = std::min(rows, sm_count() * 16);
+    cube_prefix_kernel<<<pg, kPrefixThreads, 0, st>>>(in.ssp_flux, rows, in.n_wave,
+                                                      in.ssp_wave_z, L.prefix);
     RUBIX_LAUNCH_CHECK("cube_prefix_kernel");
   }
   if (in.n > 0) {
@@ -385,7 +402,9 @@ inline int cube_prepare(const CubeInputs& in, const CubeLayout& L, const CubeTun
                                           in.vel_comp, in.perm, in.seg_off, in.n_seg, in.n,
                                           in.ssp_met, in.n_met, in.ssp_age, in.n_age,
                                           in.ssp_wave_z, in.n_wave, in.wave_t, in.n_wave_t,
-                                          L.prefix, L.ctrl, L.rec, with_grad ? 1 : 0, in.av);
+                                          L.prefix, L.ctrl, L.rec, with_grad ? 1 : 0, in.av,
+                                          (float)std::exp(-kVmaxKms / kSpeedOfLight),
+                                          (float)std::exp(kVmaxKms / kSpeedOfLight));
     RUBIX_LAUNCH_CHECK("cube_gather_kernel");
   }
   {

@@ -80,7 +80,7 @@ __global__ void resample_rows_kernel(const float* __restrict__ spec, long long s
   float* s_f = s_buf + nW;
   const float t_lo = wave_t[0], t_hi = wave_t[nT - 1];
   for (long long i = blockIdx.x; i < n; i += gridDim.x) {
-    const float alpha = (float)exp((double)vel[i * vel_stride + vel_comp] / kSpeedOfLight);
+    const float alpha = doppler_factor(vel[i * vel_stride + vel_comp]);
     const float* F = spec + i * spec_stride;
     __syncthreads();
     for (int k = threadIdx.x; k < nW; k += blockDim.x) {
