@@ -103,9 +103,9 @@ def flops_per_particle_lambda(w):
     return 7.4 + 11.0 * n_e / float(w.wave_t.size)
 
 
-def traffic_per_launch(n_particles):
-    """DRAM bytes per rubix_cube_fwd launch from the committed ncu summary, scaled to
-    the particle count of this run (the summary states the captured count)."""
+def _profile_per_launch(n_particles, total_key, fixed_key):
+    """A per-launch count of the main kernel from the committed ncu summary (fixed part +
+    per-particle part), scaled to the particle count of this run."""
     try:
         vals = {}
         with open(TRAFFIC_FILE) as f:
@@ -113,12 +113,23 @@ def traffic_per_launch(n_particles):
                 if ":" in line and not line.startswith("#"):
                     k, v = line.split(":", 1)
                     vals[k.strip()] = v.strip().split()[0]
-        b = float(vals["dram_bytes_per_launch"])
+        b = float(vals[total_key])
         n_cap = float(vals["captured_particles"])
-        fixed = float(vals.get("fixed_bytes", 0.0))
+        fixed = float(vals.get(fixed_key, 0.0))
         return fixed + (b - fixed) * n_particles / n_cap
     except Exception:
         return None
+
+
+def traffic_per_launch(n_particles):
+    """DRAM bytes per rubix_cube_fwd main-kernel launch (ncu, scaled to the run)."""
+    return _profile_per_launch(n_particles, "dram_bytes_per_launch", "fixed_bytes")
+
+
+def instructions_per_launch(n_particles):
+    """Warp instructions per main-kernel launch (ncu smsp__inst_executed.sum, scaled)."""
+    return _profile_per_launch(n_particles, "warp_instructions_per_launch",
+                               "fixed_warp_instructions")
 
 
 class ClockSampler:
@@ -824,10 +835,24 @@ def main():
                "(rubix_fma_probe)", "achieved_tflops": fp32_achieved,
                "frac": fp32_achieved / fp32_peak if fp32_peak else None,
                "flops_per_particle_lambda": fpl}
+    # instruction issue, the resource the main kernel is bound by: warp instructions per
+    # launch (ncu count, scaled to N) over the launch time, against one instruction per
+    # cycle per scheduler (4 per SM) at the SM clock sampled during the timed region
+    insts = instructions_per_launch(N)
+    issue = None
+    if insts:
+        sm_mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_issue = n_sm * 4 * sm_mhz * 1e6
+        issue = {"warp_instructions_per_launch": insts, "achieved_per_s": insts / cube_avg_s,
+                 "peak_per_s": peak_issue, "frac": insts / cube_avg_s / peak_issue,
+                 "source": "smsp__inst_executed.sum of profiles/cube_fwd_ifu.txt scaled to "
+                           f"{N} particles; peak = {n_sm} SMs x 4 schedulers x 1 warp "
+                           f"instruction per cycle at {sm_mhz:.0f} MHz"}
     roofline = {"kernel": "rubix_cube_fwd (fused lookup/mass/Doppler/resample/accumulate)",
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                "traffic": traffic, "algorithmic_bytes": alg_bytes, "issue": issue,
                 "ms_per_launch": statistics.mean(cube_ms),
                 "share_of_step": statistics.mean(cube_ms) / statistics.mean(step_ms),
                 "fp32": compute}
