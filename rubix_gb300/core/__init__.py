@@ -9,6 +9,8 @@ from .config import get_config, get_pipeline_config, rubix_config  # noqa: F401
 from .data import (Galaxy, GasData, RubixData, StarsData, get_reshape_data,  # noqa: F401
                    reshape_array)
 from .dust import apply_spaxel_extinction, get_extinction  # noqa: F401
+from .galaxy_file import (center_particles, create_rubix_file, get_rubix_data,  # noqa: F401
+                          load_galaxy_data, prepare_input)
 from .ifu import (get_calculate_datacube, get_calculate_spectra,  # noqa: F401
                   get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
 from .lsf import get_convolve_lsf  # noqa: F401

@@ -1,8 +1,9 @@
 """RubixPipeline (rubix/core/pipeline.py:30-208), eager, on the rubix_gb300 kernels.
 
 Differences from rubix, all outside the particle -> cube path: the particle data is
-passed in (``data=``, with ``galaxy.halfmassrad_stars`` for the rotation) instead of
-being read from simulation files; the SSP lookup is bilinear (``ssp.method =
+passed in (``data=``, with ``galaxy.halfmassrad_stars`` for the rotation) or read from a
+galaxy already in rubix's file format (``<output_path>/rubix_galaxy.h5``), not converted
+from simulation snapshots; the SSP lookup is bilinear (``ssp.method =
 "linear"``); the noise of ``apply_noise`` comes from a seeded Philox generator instead
 of jax.random.
 """
@@ -17,6 +18,7 @@ from ..pipeline import LinearTransformerPipeline, step_names
 from .config import get_config, get_pipeline_config
 from .data import RubixData, get_reshape_data
 from .dust import get_extinction
+from .galaxy_file import get_rubix_data
 from .ifu import (get_calculate_datacube, get_calculate_spectra,
                   get_doppler_shift_and_resampling, get_scale_spectrum_by_mass)
 from .lsf import LsfHandoff, get_convolve_lsf, lsf_fusable
@@ -43,8 +45,8 @@ class RubixPipeline:
         self.logger = get_logger(self.user_config.get("logger"))
         self.ssp = get_ssp(self.user_config)
         self.telescope = get_telescope(self.user_config)
-        if data is None:
-            raise ValueError("rubix_gb300.RubixPipeline needs the particle data (data=RubixData)")
+        # without data the galaxy is read at run time from <output_path>/rubix_galaxy.h5
+        # (rubix/core/pipeline.py:145-150 via get_rubix_data)
         self.data = data
         self.func = None
         self.fuse_lsf = fuse_lsf
@@ -68,6 +70,8 @@ class RubixPipeline:
 
     def run(self) -> RubixData:
         t0 = time.time()
+        if self.data is None:
+            self.data = get_rubix_data(self.user_config)
         names = step_names(self.pipeline_config)
         lsf = LsfHandoff() if self.fuse_lsf and lsf_fusable(names) else None
         frame = frame_fusion(names) if self.fuse_frame else None

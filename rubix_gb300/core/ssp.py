@@ -6,8 +6,8 @@ seeded synthetic generator (name ``"synthetic"``, parameters under
 ``config["ssp"]["template"]``); or one of rubix's named templates read from its file in
 the template directory (``RUBIX_GB300_TEMPLATE_PATH``, default ``templates/`` next to
 this package).  Files in rubix's pyPipe3D FITS format (MaStar, .fits or .fits.gz) are
-read with the package's own FITS reader; HDF5 templates (BC03, FSPS) need h5py, which is
-not available, and are refused with that reason.  Nothing is downloaded.
+read with the package's own FITS reader, HDF5 templates (BC03, FSPS) with its own HDF5
+reader (``rubix_gb300.hdf5``).  Nothing is downloaded.
 """
 
 from __future__ import annotations
@@ -20,6 +20,7 @@ import numpy as np
 import torch
 
 from .. import fits as fitsio
+from .. import hdf5
 from .. import ops, synth
 from ..logging import get_logger
 from .data import device_of, flat_particles, like_input
@@ -159,19 +160,32 @@ def load_pypipe3d(path: str, fields: dict = None) -> SSPGrid:
     return SSPGrid(**out)
 
 
+def load_hdf5_template(path: str, fields: dict = None) -> SSPGrid:
+    """HDF5SSPGrid.from_file (grid.py:304-335): dataset ``fields[f]["name"]`` of each
+    field, 10**data when ``in_log``, float32, converted to the internal units."""
+    out = {}
+    with hdf5.File(path, "r") as f:
+        for name, info in (fields or _FIELDS).items():
+            d = np.asarray(f[info["name"]][()], dtype=np.float64)
+            if info.get("in_log"):
+                d = np.power(10.0, d)
+            d = d.astype(np.float32)
+            out[name] = convert_units(d, name, info.get("units", SSP_UNITS[name]))
+    return SSPGrid(**out)
+
+
 def load_ssp_file(name: str) -> SSPGrid:
     """spectra/ssp/factory.py:13-76 for the templates rubix names, from the template
     directory."""
     cfg = SSP_TEMPLATES[name]
     path = os.path.join(template_path(), cfg["file_name"])
     fmt = cfg["format"].lower()
-    if fmt in ("hdf5", "fsps"):
-        raise ValueError(f"SSP template {name} is an HDF5 file ({cfg['file_name']}); reading "
-                         "HDF5 needs h5py, which is not available")
     if not os.path.exists(path):
         raise FileNotFoundError(f"SSP template file {path} not found (templates are not "
                                 "downloaded; place the file there or set "
                                 "RUBIX_GB300_TEMPLATE_PATH)")
+    if fmt in ("hdf5", "fsps"):
+        return load_hdf5_template(path, cfg["fields"])
     return load_pypipe3d(path, cfg["fields"])
 
 
@@ -226,4 +240,5 @@ def get_lookup_interpolation(config: dict) -> Callable:
 
 __all__ = ["SSPGrid", "register_ssp_template", "get_ssp", "get_ssp_template",
            "get_lookup_interpolation", "like_input", "load_pypipe3d", "load_ssp_file",
-           "SSP_TEMPLATES", "SSP_UNITS", "convert_units", "template_path"]
+           "SSP_TEMPLATES", "SSP_UNITS", "convert_units", "template_path",
+           "load_hdf5_template"]

@@ -139,7 +139,7 @@ def test_pypipe3d_loader(tmp_path, monkeypatch):
     os.replace(p, tmp_path / "MaStar_CB19.slog_1_5.fits.gz")
     g2 = ssp.get_ssp_template("Mastar_CB19_SLOG_1_5")
     np.testing.assert_array_equal(g2.flux, g.flux)
-    with pytest.raises(ValueError, match="h5py"):
+    with pytest.raises(FileNotFoundError, match="BC03lr.h5 not found"):
         ssp.get_ssp_template("BruzualCharlot2003")
 
 

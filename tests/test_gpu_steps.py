@@ -214,3 +214,41 @@ def test_host_stream_matches_render():
         p = ws[k % 3].particles
         ref = rnd.render(p.coords, p.velocity, p.mass, p.metallicity, p.age).final.cpu()
         assert torch.equal(outs[k], ref), f"galaxy {k}"
+
+
+def test_rubix_pipeline_from_galaxy_file(tmp_path):
+    """RubixPipeline(config) without data reads <output_path>/rubix_galaxy.h5
+    (get_rubix_data: load, centre) and renders the same cube as the same centred arrays
+    passed in directly."""
+    import torch
+
+    from rubix_gb300.core import (Galaxy, RubixData, RubixPipeline, StarsData,
+                                  create_rubix_file)
+
+    w = workload("small")
+    p = w.particles
+    center = np.array([0.25, -0.5, 0.1])
+    v0 = np.array([12.0, -7.0, 30.0])
+    create_rubix_file(
+        str(tmp_path / "rubix_galaxy.h5"),
+        {"stars": {"coords": p.coords + center, "velocity": p.velocity + v0, "mass": p.mass,
+                   "metallicity": p.metallicity, "age": p.age}},
+        {"center": center, "halfmassrad_stars": np.float64(HALFMASS_RADIUS),
+         "redshift": np.float64(0.0)},
+        {"simulation": "synthetic"},
+        {"galaxy": {"center": "kpc", "halfmassrad_stars": "kpc", "redshift": ""},
+         "stars": {"coords": "kpc", "velocity": "km/s", "mass": "Msun", "metallicity": "",
+                   "age": "Gyr"}})
+    cfg = _config(w)
+    cfg["output_path"] = str(tmp_path)
+    got = RubixPipeline(cfg).run().stars.datacube
+    coords = p.coords + center
+    vel = p.velocity + v0
+    near = np.linalg.norm(coords - center, axis=1) < 10
+    direct = RubixData(galaxy=Galaxy(halfmassrad_stars=HALFMASS_RADIUS),
+                       stars=StarsData(coords=coords - center,
+                                       velocity=vel - np.median(vel[near], axis=0),
+                                       mass=p.mass, metallicity=p.metallicity, age=p.age))
+    want = RubixPipeline(cfg, direct).run().stars.datacube
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)

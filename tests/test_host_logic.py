@@ -95,6 +95,8 @@ def test_ssp_config_errors_and_method():
     with pytest.raises(ValueError, match="does not contain 'name' field"):
         get_ssp({"ssp": {"template": {}}})
     with pytest.raises(ValueError, match="not available"):
+        get_ssp({"ssp": {"template": {"name": "NoSuchTemplate"}}})
+    with pytest.raises(FileNotFoundError, match="BC03lr.h5 not found"):
         get_ssp({"ssp": {"template": {"name": "BruzualCharlot2003"}}})
     cfg = {"ssp": {"template": {"name": "synthetic", "n_age": 4, "n_met": 3, "n_wave": 50}}}
     with pytest.raises(ValueError, match="method='linear'"):
@@ -161,8 +163,10 @@ def test_renderer_and_pipeline_need_cuda_and_data():
         IFURenderer.from_workload(w, device="cpu")
     cfg = {"pipeline": {"name": "calc_ifu"}, "telescope": {"name": "MUSE"},
            "ssp": {"template": {"name": "synthetic"}, "method": "linear"}}
-    with pytest.raises(ValueError, match="needs the particle data"):
-        RubixPipeline(cfg)
+    with pytest.raises(ValueError, match="no particle data"):
+        RubixPipeline(cfg).run()
+    with pytest.raises(FileNotFoundError, match="rubix_galaxy.h5 not found"):
+        RubixPipeline(dict(cfg, output_path="/nonexistent_dir")).run()
 
 
 def test_lsf_fusable_order():
