@@ -233,6 +233,119 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
                   blockIdx.y);
 }
 
+// The same strip with packed two-lane FMAs (__ffma2_rn) for host taps: the four x
+// positions of a thread form two pairs, so each tap of the x-pass and of the y-pass is
+// one FFMA2 per pair.  The x-pass operands (x_k, x_k+1) come as aligned pairs A_m =
+// (x_2m, x_2m+1) and shifted pairs B_m = (x_2m+1, x_2m+2); the taps are read from the
+// kernel parameters.  Same products and summation order as psf_reg_body, so the
+// result is bit-identical.
+template <int M>
+__global__ void __launch_bounds__(kPsfThreads, 2) psf_reg2_kernel(PsfArgs a) {
+  constexpr int W = kPsfTileX + M - 1;  // staged row width
+  constexpr int PER = (W * kPsfTileL + kPsfThreads - 1) / kPsfThreads;
+  constexpr int kPsfStages = psf_stages(M);
+  constexpr int NA = (kPsfXB + M - 1) / 2;  // aligned input pairs per thread and row
+  static_assert(kPsfXB == 4 && (M & 1), "two output pairs, odd tap count");
+  __shared__ float s_in[kPsfStages][W * kPsfTileL];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float* __restrict__ in = a.in;
+  float* __restrict__ out = a.out;
+  const int ny = a.ny, nx = a.nx, nl = a.nl, oy = a.oy;
+  const long long sin = a.sin, sout = a.sout;
+  const int x0 = blockIdx.x * kPsfTileX;
+  const int l0 = blockIdx.y * kPsfTileL;
+  const int l = l0 + lane;
+  const int xsrc0 = x0 - (M - 1) + a.ox;
+  const int xb = warp * kPsfXB;
+  const int total = ny + oy;
+  int off[PER];
+  unsigned valid = 0u;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int q = tid + k * kPsfThreads;
+    const int jj = q / kPsfTileL, ll = q % kPsfTileL;
+    const int xg = xsrc0 + jj, lg = l0 + ll;
+    const bool ok = q < W * kPsfTileL && xg >= 0 && xg < nx && lg < nl;
+    off[k] = ok ? (int)((long long)xg * sin + lg) : 0;
+    valid |= ok ? (1u << k) : 0u;
+  }
+  const long long row_stride = (long long)nx * sin;
+  auto issue_row = [&](int r) {
+    float* dst = s_in[r % kPsfStages];
+    const float* base = in + (long long)r * row_stride;
+    const bool row_ok = r < ny;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int q = tid + k * kPsfThreads;
+      if (q < W * kPsfTileL) {
+        const bool ok = row_ok && ((valid >> k) & 1u);
+        cp_async4(dst + q, ok ? base + off[k] : in, ok);
+      }
+    }
+  };
+  float2 win[M][2];  // x-convolved rows r-M+1 .. r of this thread's two output pairs
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    win[i][0] = make_float2(0.f, 0.f);
+    win[i][1] = win[i][0];
+  }
+#pragma unroll
+  for (int r = 0; r < kPsfStages - 1; ++r) {
+    if (r < total) issue_row(r);
+    cp_async_commit();
+  }
+  for (int r0 = 0; r0 < total; r0 += M) {
+#pragma unroll
+    for (int jj = 0; jj < M; ++jj) {
+      const int r = r0 + jj;
+      if (r >= total) break;
+      cp_async_wait<kPsfStages - 2>();
+      __syncthreads();
+      {
+        const int rn = r + kPsfStages - 1;
+        if (rn < total) issue_row(rn);
+        cp_async_commit();
+      }
+      const float* row = s_in[r % kPsfStages];
+      float2 A[NA], B[NA - 1];
+#pragma unroll
+      for (int m = 0; m < NA; ++m) {
+        A[m].x = row[(xb + 2 * m) * kPsfTileL + lane];
+        A[m].y = row[(xb + 2 * m + 1) * kPsfTileL + lane];
+      }
+#pragma unroll
+      for (int m = 0; m < NA - 1; ++m) B[m] = make_float2(A[m].y, A[m + 1].x);
+      float2 h0 = make_float2(0.f, 0.f), h1 = h0;
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        const float2 t = make_float2(a.tx[i], a.tx[i]);
+        const int k0 = M - 1 - i, k1 = M + 1 - i;  // first input of outputs 0-1 and 2-3
+        h0 = __ffma2_rn(t, (k0 & 1) ? B[k0 >> 1] : A[k0 >> 1], h0);
+        h1 = __ffma2_rn(t, (k1 & 1) ? B[k1 >> 1] : A[k1 >> 1], h1);
+      }
+      win[jj][0] = h0;
+      win[jj][1] = h1;
+      const int y = r - oy;
+      if (y >= 0 && l < nl) {
+        float2 o0 = make_float2(0.f, 0.f), o1 = o0;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const float2 t = make_float2(a.ty[i], a.ty[i]);
+          o0 = __ffma2_rn(t, win[(jj - i + M) % M][0], o0);
+          o1 = __ffma2_rn(t, win[(jj - i + M) % M][1], o1);
+        }
+        const int x = x0 + xb;
+        float* o = out + ((long long)y * nx + x) * sout + l;
+        if (x < nx) o[0] = o0.x;
+        if (x + 1 < nx) o[sout] = o0.y;
+        if (x + 2 < nx) o[2 * sout] = o1.x;
+        if (x + 3 < nx) o[3 * sout] = o1.y;
+      }
+    }
+  }
+  cp_async_wait<0>();
+}
+
 // Ragged batch: galaxy g owns blocks [block_off[g], block_off[g+1]) (x strips fastest),
 // its square S_g x S_g cube starts at spaxel seg_base[g], and its taps are
 // taps[g][0][:] (y) and taps[g][1][:] (x), zero-padded and centred to M.
@@ -269,6 +382,13 @@ __global__ void __launch_bounds__(kPsfThreads) ragged_psf_kernel(RaggedPsfArgs a
 template <int M>
 int launch_psf_reg(const PsfArgs& a, cudaStream_t st) {
   dim3 grid(div_up(a.nx, kPsfTileX), div_up(a.nl, kPsfTileL));
+  // host taps: the packed-FMA kernel with the taps as parameters (up to 17 taps, where
+  // its window stays in registers)
+  if (a.ty_dev == nullptr && M <= 17) {
+    psf_reg2_kernel<(M <= 17 ? M : 17)><<<grid, kPsfThreads, 0, st>>>(a);
+    RUBIX_LAUNCH_CHECK("psf_reg2_kernel");
+    return RUBIX_OK;
+  }
   psf_reg_kernel<M><<<grid, kPsfThreads, 0, st>>>(a);
   RUBIX_LAUNCH_CHECK("psf_reg_kernel");
   return RUBIX_OK;
