@@ -58,7 +58,7 @@ struct AdjArgs {
 };
 
 struct AdjSmem {
-  size_t wz, bucket, grid, stage, row_a, row_b, red, rec, total;
+  size_t wz, bucket, grid, stage, row_a, row_b, red, rec, perm, total;
 };
 
 __host__ __device__ inline AdjSmem adj_smem_layout(int n_wave, int n_grid, int row_cap,
@@ -74,6 +74,7 @@ __host__ __device__ inline AdjSmem adj_smem_layout(int n_wave, int n_grid, int r
   L.row_b = o;  o = al(o + sizeof(float4) * (size_t)row_cap);
   L.red = o;    o = al(o + sizeof(float) * 2 * kAdjWarps * kAdjSums);
   L.rec = o;    o = al(o + sizeof(ParticleRec) * kMaxChunk);
+  L.perm = o;   o = al(o + sizeof(int) * kMaxChunk);
   L.total = o;
   return L;
 }
@@ -152,7 +153,7 @@ __device__ __forceinline__ void adj_build(const AdjArgs& a, const ParticleRec& r
       float inv = 0.f;
       if (k >= 0 && k + 1 < nW) {
         const float dl = lp_next - lp;
-        inv = dl > 0.f ? 1.f / dl : 0.f;
+        inv = dl > 0.f ? __fdividef(1.f, dl) : 0.f;
       }
       const float lpw = (k + 1 >= nW) ? kFltMax : lp_next;
       row_a[e] = make_float4(lp, (G_next - G) * inv, G, lpw);
@@ -274,6 +275,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
   float4* s_rb = reinterpret_cast<float4*>(smem + SL.row_b);
   float* s_red = reinterpret_cast<float*>(smem + SL.red);  // [2][warps][8]
   ParticleRec* s_rec = reinterpret_cast<ParticleRec*>(smem + SL.rec);
+  int* s_perm = reinterpret_cast<int*>(smem + SL.perm);  // particle index of each record
   __shared__ uint64_t s_bar;
   __shared__ int s_item, s_fail;
   __shared__ float4 s_wt[2][2];  // mixing / derivative weights of the current, next particle
@@ -321,7 +323,10 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
     const float* adj = a.adj + (long long)s * a.adj_stride;
 #pragma unroll
     for (int r = 0; r < R; ++r) h[r] = (t0 + r < n_t) ? adj[t0 + r] : 0.f;
-    for (int i = tid; i < np; i += kAdjThreads) s_rec[i] = a.rec[jb + i];
+    for (int i = tid; i < np; i += kAdjThreads) {
+      s_rec[i] = a.rec[jb + i];
+      s_perm[i] = a.perm[jb + i];
+    }
     __syncthreads();
     if (np > 0 && tid == 0) {
       if (staged) adj_issue(a, s_rec[0], s_stage, &s_bar);
@@ -398,7 +403,9 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
             // dI/dv = -lambda * slope / c, dT/dv = T / c
             gv = fmaf(-beta * inv_c, HV, gamma * k * inv_c * (T + sc * DV));
           }
-          const long long i = a.perm[jb + p];
+          // the index comes from shared memory: a global load here would hold warp 0,
+          // and with it the next particle's barrier, for a memory round trip
+          const long long i = s_perm[p];
           if (a.g_mass) a.g_mass[i] = gm;
           if (a.g_met) a.g_met[i] = gz;
           if (a.g_age) a.g_age[i] = ga;
