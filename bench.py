@@ -57,7 +57,7 @@ def parse_args():
     ap.add_argument("--extras", default=None, metavar="NAMES",
                     help="comma-separated subset of the extra measurements (fwd_bwd, "
                          "plain_gpu, plain_gpu_fwd_bwd, dusty, fits_layout, noise, "
-                         "pipeline_api, ragged); default all")
+                         "galaxy_file, pipeline_api, ragged); default all")
     ap.add_argument("--ssp-wave", type=int, default=None, metavar="N",
                     help="synthetic SSP grid with N wavelengths (e.g. 5994, FSPS-sized)")
     ap.add_argument("--dust", type=int, default=0, metavar="N_GAS",
@@ -476,6 +476,52 @@ def pipeline_bench(dev, w, steps, warmup, flush):
                     "inside the timed region"}
 
 
+def galaxy_file_bench(dev, w, steps):
+    """rubix's galaxy file of the workload's particles (rubix_galaxy.h5, written once,
+    untimed) read back through get_rubix_data (HDF5 read, centring, median velocity)
+    and uploaded to the device; host wall time per load."""
+    import shutil
+    import tempfile
+    import time
+
+    import torch
+
+    from rubix_gb300.core import create_rubix_file, get_rubix_data
+
+    p = w.particles
+    tmp = tempfile.mkdtemp(prefix="rubix_galaxy_")
+    try:
+        path = create_rubix_file(
+            os.path.join(tmp, "rubix_galaxy.h5"),
+            {"stars": {"coords": p.coords, "velocity": p.velocity, "mass": p.mass,
+                       "metallicity": p.metallicity, "age": p.age}},
+            {"center": np.zeros(3), "halfmassrad_stars": np.float64(5.0),
+             "redshift": np.float64(w.dist_z)}, {"simulation": "synthetic"},
+            {"galaxy": {"center": "kpc", "halfmassrad_stars": "kpc", "redshift": ""},
+             "stars": {"coords": "kpc", "velocity": "km/s", "mass": "Msun",
+                       "metallicity": "", "age": "Gyr"}})
+        nbytes = os.path.getsize(path)
+        cfg = {"output_path": tmp, "data": {"args": {"particle_type": ["stars"]}},
+               "logger": {"log_level": "WARNING"}}
+        ts = []
+        for _ in range(steps + 1):
+            t0 = time.perf_counter()
+            d = get_rubix_data(cfg)
+            st = d.stars
+            on_dev = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+                      for a in (st.coords, st.velocity, st.mass, st.metallicity, st.age)]
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+            del on_dev
+        ms = statistics.median(ts[1:]) * 1e3
+        return {"what": "get_rubix_data(config) on a rubix_galaxy.h5 of the workload "
+                        "(rubix_gb300.hdf5 reader, centring) + upload of the five arrays",
+                "file_bytes": nbytes, "ms": ms, "mb_per_s": nbytes / (ms * 1e-3) / 1e6,
+                "particles": p.n}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def noise_bench(dev, cube, steps, warmup, flush):
     """apply_noise (S/N 20, normal draws) on a copy of the final cube: the flux image,
     the median select and the noise pass; the noise kernel's algorithmic bytes are 2 C
@@ -881,6 +927,7 @@ def main():
                 ("dusty", lambda: dusty_bench(dev, w, d_in, args.steps, 3, flush)),
                 ("fits_layout", lambda: fits_bench(dev, ours_final, args.steps, 3, flush)),
                 ("noise", lambda: noise_bench(dev, ours_final, args.steps, 3, flush)),
+                ("galaxy_file", lambda: galaxy_file_bench(dev, w, 3)),
                 ("pipeline_api", lambda: pipeline_bench(dev, w, min(args.steps, 5), 3, flush)),
                 ("ragged", lambda: ragged_bench(dev, 3, 2))):
             if args.extras is not None and name not in args.extras.split(","):

@@ -79,14 +79,28 @@ def load_galaxy_data(path_to_file: str) -> Tuple[dict, dict]:
     return galaxy_data, units
 
 
+def _jax_default(a: np.ndarray) -> np.ndarray:
+    """The dtype jnp.array gives with 64-bit types disabled (rubix's setting): float64
+    -> float32, int64 -> int32."""
+    a = np.asarray(a)
+    if a.dtype == np.float64:
+        return a.astype(np.float32)
+    if a.dtype == np.int64:
+        return a.astype(np.int32)
+    if a.dtype == np.uint64:
+        return a.astype(np.uint32)
+    return a
+
+
 def center_particles(rubixdata: RubixData, key: str) -> RubixData:
     """rubix/galaxy/alignment.py:10-62: coordinates relative to the galaxy centre,
     velocities relative to the median velocity of the particles within 10 (kpc) of it;
-    a centre outside the particles' bounding box is an error."""
+    a centre outside the particles' bounding box is an error.  In the particles' own
+    precision (float32 in rubix), the centre cast to it."""
     comp = rubixdata.stars if key == "stars" else rubixdata.gas
     coords = np.asarray(comp.coords)
     vel = np.asarray(comp.velocity)
-    center = np.asarray(rubixdata.galaxy.center)
+    center = np.asarray(rubixdata.galaxy.center, dtype=coords.dtype)
     inside = all(coords[:, i].min() <= center[i] <= coords[:, i].max() for i in range(3))
     if not inside:
         raise ValueError("Center is not within the bounds of the galaxy")
@@ -117,7 +131,7 @@ def prepare_input(config: Union[dict, str]) -> RubixData:
             continue
         comp = getattr(rubixdata, part_type)
         for attribute, value in data["particle_data"][part_type].items():
-            setattr(comp, attribute, np.asarray(value))
+            setattr(comp, attribute, _jax_default(value))  # rubix: jnp.array(value)
             setattr(comp, attribute + "_unit", units[part_type][attribute])
         logger.info(f"Centering {part_type} particles")
         rubixdata = center_particles(rubixdata, part_type)

@@ -23,6 +23,8 @@ newer chunk indexes are refused with an error naming the feature.
 
 from __future__ import annotations
 
+import mmap
+import os
 import struct
 import zlib
 from typing import Dict, Iterator, Optional, Union
@@ -376,7 +378,7 @@ class _Reader:
 
         def name_at(off):
             s = seg + off
-            return self.b[s:self.b.index(b"\x00", s)].decode("utf-8")
+            return self.b[s:self.b.find(b"\x00", s)].decode("utf-8")
 
         def walk(node):
             p = self.abs(node)
@@ -557,9 +559,11 @@ class File(Group):
     def __init__(self, path: str, mode: str = "r"):
         if mode != "r":
             raise ValueError("hdf5.File reads only; write files with hdf5.write_file")
+        # memory-mapped: a dataset read touches only its own bytes
         with open(path, "rb") as f:
-            data = f.read()
-        r = _Reader(data)
+            size = os.fstat(f.fileno()).st_size
+            self._map = mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ) if size else b""
+        r = _Reader(self._map)
         super().__init__(r, r.root, "/", r.root_scratch)
         self.filename = path
 
@@ -567,10 +571,13 @@ class File(Group):
         return self
 
     def __exit__(self, *exc):
+        self.close()
         return False
 
     def close(self):
-        pass
+        """Datasets already read stay valid (they are copies)."""
+        if isinstance(self._map, mmap.mmap) and not self._map.closed:
+            self._map.close()
 
 
 # ---------------------------------------------------------------------- writing

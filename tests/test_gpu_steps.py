@@ -242,11 +242,14 @@ def test_rubix_pipeline_from_galaxy_file(tmp_path):
     cfg = _config(w)
     cfg["output_path"] = str(tmp_path)
     got = RubixPipeline(cfg).run().stars.datacube
-    coords = p.coords + center
-    vel = p.velocity + v0
-    near = np.linalg.norm(coords - center, axis=1) < 10
+    # the file holds float64; prepare_input gives float32 (rubix's jnp.array) and
+    # centres in float32
+    coords = (p.coords + center).astype(np.float32)
+    vel = (p.velocity + v0).astype(np.float32)
+    c32 = center.astype(np.float32)
+    near = np.linalg.norm(coords - c32, axis=1) < 10
     direct = RubixData(galaxy=Galaxy(halfmassrad_stars=HALFMASS_RADIUS),
-                       stars=StarsData(coords=coords - center,
+                       stars=StarsData(coords=coords - c32,
                                        velocity=vel - np.median(vel[near], axis=0),
                                        mass=p.mass, metallicity=p.metallicity, age=p.age))
     want = RubixPipeline(cfg, direct).run().stars.datacube

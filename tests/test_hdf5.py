@@ -165,14 +165,17 @@ def test_prepare_input_centres_and_subsets(tmp_path):
     cfg = {"output_path": str(tmp_path), "data": {"args": {"particle_type": ["stars", "gas"]}},
            "logger": {"log_level": "WARNING"}}
     d = get_rubix_data(cfg)
-    c = galaxy["center"]
+    c = galaxy["center"].astype(np.float32)
     for ptype in ("stars", "gas"):
         comp = getattr(d, ptype)
-        src = particles[ptype]
-        # alignment.py:52-60: median velocity of the particles within 10 kpc of the centre
+        src = {k: v.astype(np.float32) for k, v in particles[ptype].items()}
+        # float32 as rubix (jnp.array without 64-bit types); alignment.py:52-60: median
+        # velocity of the particles within 10 kpc of the centre
+        assert comp.coords.dtype == np.float32 and comp.mass.dtype == np.float32
         near = np.linalg.norm(src["coords"] - c, axis=1) < 10
-        np.testing.assert_allclose(comp.coords, src["coords"] - c)
-        np.testing.assert_allclose(comp.velocity, src["velocity"] - np.median(src["velocity"][near], 0))
+        assert np.array_equal(comp.coords, src["coords"] - c)
+        assert np.array_equal(comp.velocity,
+                              src["velocity"] - np.median(src["velocity"][near], 0))
         assert comp.coords_unit == "kpc" and comp.mass_unit == "Msun"
     assert d.galaxy.halfmassrad_stars == 4.5 and d.galaxy.center_unit == "kpc"
     # rubix's subset: np.random.seed(42) choice without replacement over the stars
@@ -181,10 +184,10 @@ def test_prepare_input_centres_and_subsets(tmp_path):
     s = get_rubix_data(cfg)
     np.random.seed(42)
     idx = np.random.choice(np.arange(500), size=100, replace=False)
-    np.testing.assert_allclose(s.stars.mass, particles["stars"]["mass"][idx])
+    assert np.array_equal(s.stars.mass, particles["stars"]["mass"].astype(np.float32)[idx])
     np.random.seed(42)
     idx = np.random.choice(np.arange(100), size=100, replace=False)
-    np.testing.assert_allclose(s.gas.mass, particles["gas"]["mass"][idx])
+    assert np.array_equal(s.gas.mass, particles["gas"]["mass"].astype(np.float32)[idx])
     # a centre outside the particles is refused (alignment.py:38-49)
     galaxy["center"] = np.array([1e3, 0.0, 0.0])
     create_rubix_file(str(tmp_path / "rubix_galaxy.h5"), particles, galaxy, {}, units)
