@@ -87,7 +87,8 @@ def to_device(x, device, dtype=torch.float32) -> torch.Tensor:
     else:
         t = torch.from_numpy(np.ascontiguousarray(np.asarray(x)))
     if dtype is not None and t.dtype != dtype:
-        t = t.to(dtype)
+        # a bool mask is read as uint8 without a copy (same one-byte storage)
+        t = t.view(dtype) if (t.dtype == torch.bool and dtype == torch.uint8) else t.to(dtype)
     if t.device != device:
         t = t.to(device)
     return t.contiguous()
