@@ -886,7 +886,7 @@ def main():
     # instruction issue, the resource the main kernel is bound by: warp instructions per
     # launch (ncu count, scaled to N) over the launch time, against one instruction per
     # cycle per scheduler (4 per SM) at the SM clock sampled during the timed region
-    insts = instructions_per_launch(N)
+    insts = instructions_per_launch(N) if not dusty else None  # profile: dust-free kernel
     issue = None
     if insts:
         sm_mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
