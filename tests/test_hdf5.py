@@ -193,3 +193,50 @@ def test_prepare_input_centres_and_subsets(tmp_path):
     create_rubix_file(str(tmp_path / "rubix_galaxy.h5"), particles, galaxy, {}, units)
     with pytest.raises(ValueError, match="Center is not within the bounds"):
         get_rubix_data(dict(cfg, data={"args": {"particle_type": ["stars"]}}))
+
+
+def _ohdr(msgs):
+    """A version-2 object header ("OHDR", no times, 4-byte chunk size, a zero
+    checksum: the reader does not verify checksums) holding (type, body) messages."""
+    import struct
+
+    body = b"".join(struct.pack("<BHB", t, len(d), 0) + d for t, d in msgs)
+    return b"OHDR" + struct.pack("<BBI", 2, 0x02, len(body)) + body + b"\0\0\0\0"
+
+
+def test_reads_version2_superblock_and_object_headers(tmp_path):
+    """Superblock 2, version-2 object headers, a compact group of link messages, a
+    version-2 dataspace, a version-3 attribute and a compact data layout: the layout
+    newer HDF5 libraries write (checked against the file format specification)."""
+    import struct
+
+    und = 0xFFFFFFFFFFFFFFFF
+    data = np.arange(6, dtype="<f4").reshape(2, 3)
+    f32 = struct.pack("<BBBBI", 0x11, 0x20, 31, 0, 4) + struct.pack("<HHBBBBI", 0, 32, 23, 8,
+                                                                    0, 23, 127)
+    space = struct.pack("<BBBB", 2, 2, 0, 1) + struct.pack("<QQ", 2, 3)
+    layout = struct.pack("<BBH", 3, 0, data.nbytes) + data.tobytes()  # compact
+    sdt = struct.pack("<BBBBI", 0x13, 0, 0, 0, 3)  # fixed string of 3 bytes
+    scal = struct.pack("<BBBB", 2, 0, 0, 0)
+    attr = (struct.pack("<BBHHHB", 3, 0, 5, len(sdt), len(scal), 0) + b"unit\0" + sdt + scal
+            + b"kpc")
+    ds = _ohdr([(0x01, space), (0x03, f32), (0x08, layout), (0x0C, attr)])
+    sb_size = 8 + 4 + 4 * 8 + 4
+    ds_addr = sb_size
+
+    def link(name, addr):
+        nb = name.encode()
+        return struct.pack("<BBB", 1, 0, len(nb)) + nb + struct.pack("<Q", addr)
+
+    root = _ohdr([(0x06, link("coords", ds_addr))])
+    root_addr = ds_addr + len(ds)
+    eof = root_addr + len(root)
+    sb = (b"\x89HDF\r\n\x1a\n" + struct.pack("<BBBB", 2, 8, 8, 0)
+          + struct.pack("<QQQQ", 0, und, eof, root_addr) + b"\0\0\0\0")
+    p = tmp_path / "v2.h5"
+    p.write_bytes(sb + ds + root)
+    f = hdf5.File(str(p))
+    assert f.keys() == ["coords"]
+    assert f["coords"].shape == (2, 3)
+    assert np.array_equal(f["coords"][()], data)
+    assert f["coords"].attrs == {"unit": "kpc"}
