@@ -644,16 +644,33 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       if constexpr (kDust) {
         // transmission 10^(-0.4 A(lambda)/A(V) A_V) of each particle's dust column
         // (spectra/dust/dust_baseclasses.py:163-164) applied to its resampled spectrum
+        // (one 2^x per particle of the batch: cnt is the same for the whole block)
         const float av0 = recs[0].c.w;
         const float av1 = cnt > 1 ? recs[1].c.w : 0.f;
         const float av2 = cnt > 2 ? recs[2].c.w : 0.f;
+        if (cnt == 3) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const float e2 = __ldg(a.dust_e2 + min(t0 + r, n_t - 1));
-          const float g0 = __fmul_rn(beta0, exp2f(__fmul_rn(e2, av0)));
-          const float g1 = __fmul_rn(beta1, exp2f(__fmul_rn(e2, av1)));
-          const float g2 = __fmul_rn(beta2, exp2f(__fmul_rn(e2, av2)));
-          acc[r] = fmaf(g2, I[2][r], fmaf(g1, I[1][r], fmaf(g0, I[0][r], acc[r])));
+          for (int r = 0; r < R; ++r) {
+            const float e2 = __ldg(a.dust_e2 + min(t0 + r, n_t - 1));
+            const float g0 = __fmul_rn(beta0, dust_transmission(e2, av0));
+            const float g1 = __fmul_rn(beta1, dust_transmission(e2, av1));
+            const float g2 = __fmul_rn(beta2, dust_transmission(e2, av2));
+            acc[r] = fmaf(g2, I[2][r], fmaf(g1, I[1][r], fmaf(g0, I[0][r], acc[r])));
+          }
+        } else if (cnt == 2) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const float e2 = __ldg(a.dust_e2 + min(t0 + r, n_t - 1));
+            const float g0 = __fmul_rn(beta0, dust_transmission(e2, av0));
+            const float g1 = __fmul_rn(beta1, dust_transmission(e2, av1));
+            acc[r] = fmaf(g1, I[1][r], fmaf(g0, I[0][r], acc[r]));
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const float e2 = __ldg(a.dust_e2 + min(t0 + r, n_t - 1));
+            acc[r] = fmaf(__fmul_rn(beta0, dust_transmission(e2, av0)), I[0][r], acc[r]);
+          }
         }
       } else {
 #pragma unroll

@@ -223,7 +223,7 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
     const float IZ = fmaf(d, f.y, f.x);
     const float IA = fmaf(d, f.w, f.z);
     float hr = h[r];
-    if constexpr (kDust) hr = __fmul_rn(hr, exp2f(__fmul_rn(__ldg(e2 + min(t0 + r, n_t - 1)), av)));
+    if constexpr (kDust) hr = __fmul_rn(hr, dust_transmission(__ldg(e2 + min(t0 + r, n_t - 1)), av));
     s[0] = fmaf(hr, I, s[0]);
     s[1] = fmaf(dlam[r], I, s[1]);
     s[2] = fmaf(hr, IZ, s[2]);

@@ -83,6 +83,16 @@ __device__ __forceinline__ float doppler_factor(float v) {
   p = fma(p, x, 1.0);
   return (float)p;
 }
+
+// The dust transmission 2^(e A_V) of a resampled spectrum at one telescope wavelength
+// (e = -0.4 log2(10) A(lambda)/A(V), rubix's 10^(-0.4 A_lambda),
+// spectra/dust/dust_baseclasses.py:163-164): one hardware 2^x (PTX ex2.approx.ftz.f32,
+// relative error about 2^-22, results below 2^-126 flushed to 0).
+__device__ __forceinline__ float dust_transmission(float e, float av) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__fmul_rn(e, av)));
+  return y;
+}
 #endif
 
 }  // namespace rubix

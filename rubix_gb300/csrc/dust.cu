@@ -343,7 +343,7 @@ __global__ void dust_rows_kernel(float* __restrict__ rows, long long n, int L,
     const long long i = k / L;
     const int t = (int)(k - i * L);
     float* p = rows + i * row_stride + t;
-    *p = __fmul_rn(*p, exp2f(__fmul_rn(e[t], av[i])));
+    *p = __fmul_rn(*p, dust_transmission(e[t], av[i]));
   }
 }
 
