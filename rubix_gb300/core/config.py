@@ -58,7 +58,13 @@ def get_config(config):
 
 
 def get_pipeline_config(name: str):
-    """rubix/utils.py:30-44."""
+    """rubix/utils.py:30-44 (a fresh copy of the named pipeline's node table)."""
     if name not in PIPELINES:
         raise ValueError(f"Pipeline {name} not found in the configuration")
-    return copy.deepcopy(PIPELINES[name])
+    src = PIPELINES[name]
+    # nodes hold name, depends_on, args (list) and kwargs (dict): copied one level deep,
+    # which is all a deep copy would copy, at a fraction of its cost
+    return {k: ({n: {f: (list(v) if isinstance(v, list) else dict(v) if isinstance(v, dict)
+                        else v) for f, v in node.items()} for n, node in val.items()}
+                if k == "Transformers" else copy.deepcopy(val))
+            for k, val in src.items()}

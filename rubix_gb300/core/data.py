@@ -85,7 +85,10 @@ def to_device(x, device, dtype=torch.float32) -> torch.Tensor:
     if isinstance(x, torch.Tensor):
         t = x
     else:
-        t = torch.from_numpy(np.ascontiguousarray(np.asarray(x)))
+        a = np.ascontiguousarray(np.asarray(x))
+        if not a.flags.writeable:  # shared read-only constants: torch wants its own copy
+            a = a.copy()
+        t = torch.from_numpy(a)
     if dtype is not None and t.dtype != dtype:
         # a bool mask is read as uint8 without a copy (same one-byte storage)
         t = t.view(dtype) if (t.dtype == torch.bool and dtype == torch.uint8) else t.to(dtype)

@@ -8,6 +8,7 @@ the reference's arithmetic and then uploaded; the kernels receive them as arrays
 
 from __future__ import annotations
 
+import functools
 import math
 from dataclasses import dataclass, field
 from typing import Optional
@@ -70,13 +71,24 @@ def create_telescope(name: str, telescopes_config: Optional[dict] = None) -> Tel
     sbin = int(np.floor(c["fov"] / c["spatial_res"]))
     if c["aperture_type"] not in ("square", "circular", "hexagonal"):
         raise ValueError(f"Unknown aperture type: {c['aperture_type']}")
-    ws = calculate_wave_seq(c["wave_range"], c["wave_res"])
+    ws, we = _wave_grids(tuple(float(x) for x in c["wave_range"]), float(c["wave_res"]))
     return Telescope(
         name=name, fov=c["fov"], spatial_res=c["spatial_res"], wave_range=list(c["wave_range"]),
         wave_res=c["wave_res"], lsf_fwhm=c["lsf_fwhm"], signal_to_noise=c["signal_to_noise"],
         sbin=sbin, pixel_type=c["pixel_type"], aperture_type=c["aperture_type"],
-        wave_seq=ws, wave_edges=calculate_wave_edges(ws, c["wave_res"]),
+        wave_seq=ws, wave_edges=we,
     )
+
+
+@functools.lru_cache(maxsize=64)
+def _wave_grids(wave_range: tuple, wave_res: float):
+    """wave_seq and wave_edges of a telescope, computed once per (range, resolution)
+    and shared read-only (every pipeline step builds the telescope)."""
+    ws = calculate_wave_seq(wave_range, wave_res)
+    we = calculate_wave_edges(ws, wave_res)
+    ws.flags.writeable = False
+    we.flags.writeable = False
+    return ws, we
 
 
 # ------------------------------------------------------------------ cosmology
@@ -84,6 +96,7 @@ PLANCK15 = dict(Om0=0.3075, w0=-1.0, wa=0.0, h=0.6774)  # rubix/cosmology/__init
 COSMOLOGIES = {"PLANCK15": PLANCK15}
 
 
+@functools.lru_cache(maxsize=64)
 def angular_scale(z: float, Om0=0.3075, w0=-1.0, wa=0.0, h=0.6774) -> np.float32:
     """kpc per arcsec at redshift z for flat wCDM (rubix/cosmology/base.py:121-139, 290-314):
     comoving distance by the trapezoid rule on 256 nodes of [0, z]."""
