@@ -195,3 +195,36 @@ def test_frame_fusion_order():
     assert h is not None and not h.rotation
     assert frame_fusion(["spaxel_assignment", "filter_particles"]) is None
     assert frame_fusion(["filter_particles", "x", "spaxel_assignment"]) is None
+
+
+def test_device_constants_and_read_only_arrays():
+    import torch
+
+    from rubix_gb300 import telescope as tel
+    from rubix_gb300.core.data import device_constant, to_device
+
+    cpu = torch.device("cpu")
+    a = np.linspace(0.0, 1.0, 7).astype(np.float32)
+    t1 = device_constant(a, cpu)
+    t2 = device_constant(a.copy(), cpu)  # same contents: the same uploaded tensor
+    assert t1 is t2 and torch.equal(t1, torch.from_numpy(a))
+    assert device_constant(a + 1, cpu) is not t1
+    # the telescope grids are shared read-only arrays; uploads copy them
+    t = tel.create_telescope("MUSE")
+    assert not t.wave_seq.flags.writeable
+    assert tel.create_telescope("MUSE").wave_seq is t.wave_seq
+    u = to_device(t.wave_seq, cpu)
+    u[0] = -1.0  # a copy: the shared grid is untouched
+    assert t.wave_seq[0] != -1.0
+    # a bool mask read as uint8 shares its storage (no copy)
+    m = torch.tensor([True, False, True])
+    assert to_device(m, cpu, torch.uint8).tolist() == [1, 0, 1]
+
+
+def test_rubix_default_dtypes_of_loaded_arrays():
+    from rubix_gb300.core.galaxy_file import _jax_default
+
+    assert _jax_default(np.zeros(3)).dtype == np.float32
+    assert _jax_default(np.zeros(3, np.int64)).dtype == np.int32
+    assert _jax_default(np.zeros(3, np.float32)).dtype == np.float32
+    assert _jax_default(np.zeros(3, bool)).dtype == bool
