@@ -315,19 +315,6 @@ __device__ __forceinline__ float warp_reduce4(float v0, float v1, float v2, floa
   return c;
 }
 
-// Sums 2 values over the 32 lanes with 5 shuffles; lane 0 ends with the total of v0,
-// lane 16 with the total of v1.
-__device__ __forceinline__ float warp_reduce2(float v0, float v1, int lane) {
-  const bool hi = lane & 16;
-  float c = hi ? v1 : v0;
-  c += __shfl_xor_sync(0xffffffffu, hi ? v0 : v1, 16);
-  c += __shfl_xor_sync(0xffffffffu, c, 8);
-  c += __shfl_xor_sync(0xffffffffu, c, 4);
-  c += __shfl_xor_sync(0xffffffffu, c, 2);
-  c += __shfl_xor_sync(0xffffffffu, c, 1);
-  return c;
-}
-
 // Bracket of this thread's first wavelength on a particle's row: bucket table in log
 // wavelength, then exact comparisons on lambda'.
 __device__ __forceinline__ int first_bracket(const float4* __restrict__ rowp, int ks, int ke,

@@ -378,7 +378,7 @@ DustLayout carve_dust(void* base, long long ng, int nseg) {
   L.k1 = c.take<unsigned>(n);
   L.v0 = c.take<int>(n);
   L.v1 = c.take<int>(n);
-  L.hist = c.take<int>((size_t)kRadix * radix_tiles(ng));
+  L.hist = c.take<int>((size_t)radix_hist_ints(ng));
   L.perm = c.take<int>(n);
   L.seg_off = c.take<int>((size_t)nseg + 1);
   L.cum = c.take<float>(n);

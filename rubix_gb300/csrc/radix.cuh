@@ -36,19 +36,72 @@ radix_hist_kernel(const unsigned* __restrict__ keys, long long n, int shift,
 // Stable scatter of one digit pass.  Warp w of the tile owns the contiguous keys
 // [base + w*512, base + (w+1)*512) and walks them in 16 rounds of 32, so
 // (warp, round, lane) order equals input order.
+// One block per digit: the exclusive scan of the digit's row of tile counts, in place,
+// and the row total (the digits' offsets are added by the scatter).
+__global__ void __launch_bounds__(kSortThreads)
+radix_rowscan_kernel(int* __restrict__ hist, int n_tiles, int* __restrict__ totals) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ int s_warp[kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int* row = hist + (long long)blockIdx.x * n_tiles;
+  int carry = 0;
+  for (int base = 0; base < n_tiles; base += kSortThreads) {
+    const int t = base + threadIdx.x;
+    const int v = t < n_tiles ? row[t] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    int before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      const int ws = s_warp[w];
+      before += w < warp ? ws : 0;
+      all += ws;
+    }
+    if (t < n_tiles) row[t] = carry + before + x - v;
+    carry += all;
+    __syncthreads();  // s_warp is rewritten by the next chunk
+  }
+  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
 __global__ void __launch_bounds__(kSortThreads)
 radix_scatter_kernel(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
                      unsigned* __restrict__ keys_out, int* __restrict__ vals_out, long long n,
                      int shift, unsigned digit_mask, int n_tiles,
-                     const int* __restrict__ hist_scanned) {
+                     const int* __restrict__ hist_scanned, const int* __restrict__ totals) {
   constexpr int kWarps = kSortThreads / 32;
+  static_assert(kSortThreads == kRadix, "one thread per digit for the digit offsets");
   __shared__ int s_cnt[kWarps][kRadix];
   __shared__ int s_base[kRadix];
+  __shared__ int s_dw[kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
   const int n_digits = (int)digit_mask + 1;
-  for (int d = threadIdx.x; d < n_digits; d += kSortThreads)
-    s_base[d] = hist_scanned[(long long)d * n_tiles + blockIdx.x];
+  {
+    // offset of digit d: the totals of the digits below it (exclusive block scan), plus
+    // this tile's position in d's row (already scanned)
+    const int d = threadIdx.x;
+    const int v = d < n_digits ? totals[d] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_dw[warp] = x;
+    __syncthreads();
+    int before = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) before += w < warp ? s_dw[w] : 0;
+    if (d < n_digits)
+      s_base[d] = before + x - v + hist_scanned[(long long)d * n_tiles + blockIdx.x];
+  }
   __syncthreads();
 
   const long long wbase = (long long)blockIdx.x * kSortTile + (long long)warp * (32 * kSortItems);
@@ -99,11 +152,15 @@ inline long long radix_tiles(long long n) {
   return t < 1 ? 1 : t;
 }
 
+// Ints of the histogram workspace of a sort of n keys: [digit][tile] counts, then the
+// kRadix digit totals.
+inline long long radix_hist_ints(long long n) { return (long long)kRadix * (radix_tiles(n) + 1); }
+
 // Sorts n pairs by bits [0, bits) of the keys, stably, ping-ponging between (k0, v0)
-// and (k1, v1); `hist` holds kRadix * radix_tiles(n) ints.  Returns 0 when the sorted
+// and (k1, v1); `hist` holds radix_hist_ints(n) ints.  Returns 0 when the sorted
 // pairs end in (k0, v0), 1 when in (k1, v1).  bits = 0 sorts nothing.
 inline int radix_sort_pairs(unsigned* k0, int* v0, unsigned* k1, int* v1, long long n, int bits,
-                            int* hist, cudaStream_t st) {
+                            int* hist, cudaStream_t st) {  // hist: radix_hist_ints(n) ints
   const int n_tiles = (int)radix_tiles(n);
   unsigned* kin = k0;
   unsigned* kout = k1;
@@ -112,10 +169,11 @@ inline int radix_sort_pairs(unsigned* k0, int* v0, unsigned* k1, int* v1, long l
   int where = 0;
   for (int shift = 0; shift < bits; shift += kRadixBits) {
     const unsigned dmask = (unsigned)(kRadix - 1);
+    int* totals = hist + (long long)kRadix * n_tiles;
     radix_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, n, shift, dmask, n_tiles, hist);
-    scan_exclusive_1block<<<1, 1024, 0, st>>>(hist, (long long)kRadix * n_tiles, 0);
+    radix_rowscan_kernel<<<kRadix, kSortThreads, 0, st>>>(hist, n_tiles, totals);
     radix_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, vin, kout, vout, n, shift, dmask,
-                                                           n_tiles, hist);
+                                                           n_tiles, hist, totals);
     unsigned* tk = kin;
     kin = kout;
     kout = tk;

@@ -253,7 +253,7 @@ extern "C" size_t rubix_spaxel_sort_workspace_size(int64_t n, int32_t n_segments
   c.take<unsigned>((size_t)n);               // keys A
   c.take<unsigned>((size_t)n);               // keys B
   c.take<int>((size_t)n);                    // vals scratch
-  c.take<int>((size_t)kRadix * n_tiles);     // histogram
+  c.take<int>((size_t)kRadix * (n_tiles + 1));  // histogram + digit totals
   return c.off;
 }
 
@@ -282,7 +282,8 @@ extern "C" int rubix_spaxel_sort(const int32_t* idx, const uint8_t* keep, int64_
   unsigned* keys_a = c.take<unsigned>((size_t)n);
   unsigned* keys_b = c.take<unsigned>((size_t)n);
   int* vals_ws = c.take<int>((size_t)n);
-  int* hist = c.take<int>((size_t)kRadix * n_tiles);
+  int* hist = c.take<int>((size_t)kRadix * (n_tiles + 1));
+  int* totals = hist + (long long)kRadix * n_tiles;  // per-digit totals of a pass
 
   const int passes = sort_passes(n_segments);
   // The last pass must write into perm_out: pass p writes perm_out when
@@ -299,10 +300,10 @@ extern "C" int rubix_spaxel_sort(const int32_t* idx, const uint8_t* keep, int64_
     int* vout = dst_vals(p);
     radix_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, n, shift, dmask, n_tiles, hist);
     RUBIX_LAUNCH_CHECK("radix_hist_kernel");
-    scan_exclusive_1block<<<1, 1024, 0, st>>>(hist, (long long)kRadix * n_tiles, 0);
-    RUBIX_LAUNCH_CHECK("scan_exclusive_1block");
+    radix_rowscan_kernel<<<kRadix, kSortThreads, 0, st>>>(hist, n_tiles, totals);
+    RUBIX_LAUNCH_CHECK("radix_rowscan_kernel");
     radix_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>(kin, vals_src, kout, vout, n, shift,
-                                                           dmask, n_tiles, hist);
+                                                           dmask, n_tiles, hist, totals);
     RUBIX_LAUNCH_CHECK("radix_scatter_kernel");
     unsigned* tk = kin;
     kin = kout;
