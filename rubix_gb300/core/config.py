@@ -12,6 +12,8 @@ import copy
 import json
 import os
 
+from .. import yaml_subset
+
 rubix_config = {
     "constants": {"SPEED_OF_LIGHT": 299792.458, "KPC_TO_CM": 3.08568e21,
                   "MSUN_TO_GRAMS": 1.989e33, "MASS_OF_PROTON": 1.67262e-24},
@@ -48,13 +50,18 @@ PIPELINES = {"calc_ifu": _chain(_CALC_IFU_ORDER),
 
 
 def get_config(config):
-    """A user config dict (copied) or the path of a JSON file (rubix/utils.py:10-27)."""
+    """rubix/utils.py:10-27: a user config dict (copied) or the path of a YAML file (read
+    with ``rubix_gb300.yaml_subset``, which covers what rubix's configurations use) or of
+    a JSON file (``.json``)."""
     if isinstance(config, dict):
         return copy.deepcopy(config)
     if isinstance(config, str) and os.path.exists(config):
-        with open(config) as f:
-            return json.load(f)
-    raise ValueError(f"Cannot read configuration {config!r} (a dict or a JSON file path)")
+        if config.lower().endswith(".json"):
+            with open(config) as f:
+                return json.load(f)
+        return yaml_subset.load_file(config)
+    raise ValueError(f"Cannot read configuration {config!r} (a dict or a YAML / JSON file "
+                     "path)")
 
 
 def get_pipeline_config(name: str):

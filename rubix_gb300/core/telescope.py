@@ -21,6 +21,20 @@ def register_telescope(name: str, params: dict) -> None:
     _CUSTOM[name] = dict(params)
 
 
+def register_telescopes_file(path: str) -> list:
+    """Register every telescope of a file in the layout of rubix's telescopes.yaml
+    (TelescopeFactory(telescopes_config=path), telescope/factory.py:28-36); returns the
+    names."""
+    from .. import yaml_subset
+
+    table = yaml_subset.load_file(path)
+    if not isinstance(table, dict):
+        raise ValueError(f"{path}: expected a mapping of telescope names to parameters")
+    for name, params in table.items():
+        register_telescope(name, params)
+    return list(table)
+
+
 def get_telescope(config) -> tel.Telescope:
     """rubix/core/telescope.py:20-47."""
     name = config["telescope"]["name"]
