@@ -17,6 +17,13 @@ timed region, the copies of one step overlapping the compute of the next.  The
 latency of one isolated step (``IFURenderer.render`` plus the download, nothing
 overlapped) is reported beside it.
 
+``roofline`` relates the dominant kernel to HBM (its algorithmic bytes), to the FP32
+FMA rate (its algorithmic FLOPs; measured peak) and to instruction issue (its ncu
+instruction count, the resource it is bound by).  At N = 1 the line also carries the
+extra measurements (``--extras`` selects them): forward+backward, the plain PyTorch
+GPU path, the dusty step, the FITS layout, the noise pass, a galaxy-file load, the
+RubixPipeline step API and a ragged batch of 256 galaxies.
+
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun each rank renders its own galaxy (weak scaling, no collective on the
 data path); rank 0 prints one JSON line.
