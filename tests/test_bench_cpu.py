@@ -1,0 +1,39 @@
+"""bench.py's host-side helpers (no GPU): the profile-derived per-launch figures, the
+algorithmic FLOP count, the workload description and the argument defaults."""
+
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def test_profile_figures_scale_with_the_particle_count():
+    # profiles/cube_fwd_ifu.txt: captured at 1e6 particles, fixed + per-particle parts
+    assert bench.traffic_per_launch(1_000_000) == pytest.approx(389.68e6)
+    assert bench.instructions_per_launch(1_000_000) == pytest.approx(3478.3e6)
+    # the 2e5-particle capture lies on the same line
+    assert bench.instructions_per_launch(200_000) == pytest.approx(802.3e6, rel=1e-3)
+    assert bench.traffic_per_launch(200_000) == pytest.approx(304.28e6, rel=2e-3)
+
+
+def test_workload_description_and_flops():
+    from rubix_gb300 import synth
+
+    w = synth.make_workload("small", n=100, edge_cases=False)
+    cfg = bench.workload_config(w)
+    assert cfg["n_particles"] == 100 and cfg["n_wave"] == w.wave_t.size
+    assert "flushed" in cfg["l2"]
+    f = bench.flops_per_particle_lambda(w)
+    assert 7.4 < f < 7.4 + 11.0 * w.wave_z.size / w.wave_t.size + 1e-9
+
+
+def test_argument_defaults(monkeypatch):
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    a = bench.parse_args()
+    assert (a.gpus, a.steps, a.warmup, a.impl, a.workload) == (1, 10, 3, "ours", "ifu")
+    assert a.warmup >= 3 and a.extras is None and a.dust == 0
