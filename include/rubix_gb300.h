@@ -288,12 +288,14 @@ RUBIX_API int rubix_fma_probe(float* out, int32_t iters, void* stream);
  * rubix_cube_fwd without the workspace argument, for callers that cannot allocate
  * device memory when they render: hosts that own all GPU memory through their own
  * pool and forbid cudaMalloc from plugins, or loops that must never enter an
- * allocator.  Same inputs, output and results as rubix_cube_fwd; the scratch is a
- * static device array of RUBIX_CUBE_NOALLOC_SCRATCH_BYTES that every GPU loading
- * this part of the library keeps until process exit.  Problems needing more scratch
- * (rubix_cube_workspace_size) return RUBIX_E_WORKSPACE.  The first call on a device
- * looks up the array's address (cudaGetSymbolAddress) and should come before any
- * stream capture.  All calls share the array: calls whose GPU work overlaps race.
+ * allocator.  Same inputs, output and results as rubix_cube_fwd (bit-identical); the
+ * scratch is a static device array of RUBIX_CUBE_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this part of the library keeps until process exit.  Arguments are checked
+ * as rubix_cube_fwd checks them (same codes); then problems needing more scratch
+ * (rubix_cube_workspace_size) return RUBIX_E_WORKSPACE.  The first call in a CUDA
+ * context looks up the array's address (cudaGetSymbolAddress, cached per context)
+ * and should come before any stream capture.  All calls share the array: calls whose
+ * GPU work overlaps race.
  */
 #define RUBIX_CUBE_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 RUBIX_API int rubix_cube_fwd_noalloc(const float* ssp_flux, const float* ssp_metallicity,
@@ -307,6 +309,17 @@ RUBIX_API int rubix_cube_fwd_noalloc(const float* ssp_flux, const float* ssp_met
                                      const float* lsf_taps, int32_t n_lsf_taps,
                                      int32_t lsf_crop, float* cube, int64_t spaxel_stride,
                                      void* stream);
+
+/*
+ * No counterpart in rubix (rubix has no device error word).
+ *
+ * rubix_cube_status for rubix_cube_fwd_noalloc, whose caller never holds the scratch
+ * address: reads the device error word of the last no-alloc call in the current
+ * context (synchronises `stream`).  *device_error = 1 and RUBIX_E_DEVICE if a
+ * shared-memory copy wait in the kernel gave up (that cube is invalid), else 0 /
+ * RUBIX_OK.
+ */
+RUBIX_API int rubix_cube_noalloc_status(int* device_error, void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* Materialised intermediates (step-by-step use; the fused path never needs them) */

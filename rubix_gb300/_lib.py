@@ -72,6 +72,7 @@ SIGNATURES = {
          _vp, _vp, _vp, _vp, _i64, _i32,
          _vp, _vp, _i32, _i64, _vp, _i32, _i32, _vp, _i64, _vp],
     ),
+    "rubix_cube_noalloc_status": (_c.c_int, [_c.POINTER(_c.c_int), _vp]),
     "rubix_ssp_lookup": (_c.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _i64, _vp, _i64, _vp]),
     "rubix_mask_zero": (_c.c_int, [_vp, _i64, _i32, _i64, _vp, _vp]),
     "rubix_scale_rows": (_c.c_int, [_vp, _i64, _vp, _i64, _i32, _vp, _i64, _vp]),

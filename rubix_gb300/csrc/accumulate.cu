@@ -779,17 +779,19 @@ extern "C" size_t rubix_cube_workspace_size(int64_t n, int32_t n_segments, int32
 }
 
 namespace rubix {
-namespace {
 
-int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metallicity,
-                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met, int32_t n_age,
-                  int32_t n_wave, const float* wave_t, int32_t n_wave_t, const float* mass,
-                  const float* metallicity, const float* age, const float* velocity,
-                  int64_t vel_stride, int32_t vel_component, const int32_t* perm,
-                  const int32_t* seg_offsets, int32_t n_segments, int64_t n,
-                  const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop, const float* av,
-                  const float* dust_e2, float* cube, int64_t spaxel_stride, void* workspace,
-                  size_t workspace_bytes, void* stream) {
+// The argument checks of rubix_cube_fwd that come before its workspace check, shared
+// with rubix_cube_fwd_noalloc so that both entry points return the same code for the
+// same arguments.  *nothing_to_do is set when there is no spaxel to write.
+int cube_fwd_check_args(const char* who, const float* ssp_flux, const float* ssp_metallicity,
+                        const float* ssp_age, const float* ssp_wave_z, int32_t n_met,
+                        int32_t n_age, int32_t n_wave, const float* wave_t, int32_t n_wave_t,
+                        const float* mass, const float* metallicity, const float* age,
+                        const float* velocity, int64_t vel_stride, int32_t vel_component,
+                        const int32_t* perm, const int32_t* seg_offsets, int32_t n_segments,
+                        int64_t n, const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop,
+                        const float* cube, int64_t spaxel_stride, bool* nothing_to_do) {
+  *nothing_to_do = false;
   RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "%s: bad n", who);
   RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "%s: n_segments < 0", who);
   RUBIX_REQUIRE(n_met >= 2 && n_age >= 2, RUBIX_E_SHAPE,
@@ -805,12 +807,38 @@ int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
                 "%s: at most %d LSF taps", who, kMaxLsfTaps);
   RUBIX_REQUIRE(n_lsf_taps == 0 || (lsf_taps && lsf_crop >= 0 && lsf_crop < n_lsf_taps),
                 RUBIX_E_INVALID, "%s: bad LSF taps/crop", who);
-  if (n_segments == 0) return RUBIX_OK;
+  if (n_segments == 0) {
+    *nothing_to_do = true;
+    return RUBIX_OK;
+  }
   RUBIX_REQUIRE(ssp_flux && ssp_metallicity && ssp_age && ssp_wave_z && wave_t && seg_offsets &&
                     cube,
                 RUBIX_E_INVALID, "%s: null pointer", who);
   RUBIX_REQUIRE(n == 0 || (mass && metallicity && age && velocity && perm), RUBIX_E_INVALID,
                 "%s: null particle pointer", who);
+  return RUBIX_OK;
+}
+
+namespace {
+
+int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metallicity,
+                  const float* ssp_age, const float* ssp_wave_z, int32_t n_met, int32_t n_age,
+                  int32_t n_wave, const float* wave_t, int32_t n_wave_t, const float* mass,
+                  const float* metallicity, const float* age, const float* velocity,
+                  int64_t vel_stride, int32_t vel_component, const int32_t* perm,
+                  const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                  const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop, const float* av,
+                  const float* dust_e2, float* cube, int64_t spaxel_stride, void* workspace,
+                  size_t workspace_bytes, void* stream) {
+  {
+    bool nothing_to_do = false;
+    const int rc = cube_fwd_check_args(who, ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z,
+                                       n_met, n_age, n_wave, wave_t, n_wave_t, mass,
+                                       metallicity, age, velocity, vel_stride, vel_component,
+                                       perm, seg_offsets, n_segments, n, lsf_taps, n_lsf_taps,
+                                       lsf_crop, cube, spaxel_stride, &nothing_to_do);
+    if (rc != RUBIX_OK || nothing_to_do) return rc;
+  }
   const size_t need = rubix_cube_workspace_size(n, n_segments, n_wave_t, n_met, n_age, n_wave);
   RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
                 "%s: workspace of %zu bytes needed, %zu given", who, need, workspace_bytes);
@@ -883,6 +911,24 @@ int cube_fwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
 }
 
 }  // namespace
+
+// rubix_cube_fwd under another entry point's name (error messages carry `who`).
+int cube_fwd_named(const char* who, const float* ssp_flux, const float* ssp_metallicity,
+                   const float* ssp_age, const float* ssp_wave_z, int32_t n_met, int32_t n_age,
+                   int32_t n_wave, const float* wave_t, int32_t n_wave_t, const float* mass,
+                   const float* metallicity, const float* age, const float* velocity,
+                   int64_t vel_stride, int32_t vel_component, const int32_t* perm,
+                   const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                   const float* lsf_taps, int32_t n_lsf_taps, int32_t lsf_crop, float* cube,
+                   int64_t spaxel_stride, void* workspace, size_t workspace_bytes,
+                   void* stream) {
+  return cube_fwd_impl(who, ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, n_met, n_age,
+                       n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity, vel_stride,
+                       vel_component, perm, seg_offsets, n_segments, n, lsf_taps, n_lsf_taps,
+                       lsf_crop, nullptr, nullptr, cube, spaxel_stride, workspace,
+                       workspace_bytes, stream);
+}
+
 }  // namespace rubix
 
 extern "C" int rubix_cube_fwd(const float* ssp_flux, const float* ssp_metallicity,

@@ -56,10 +56,22 @@ def test_abi_version_and_workspace_queries(rubix_lib):
     (lambda h: h.rubix_cube_fwd(None, None, None, None, 2, 5, 10, None, 5000, None, None, None,
                                 None, 3, 2, None, None, 4, 10, None, 0, 0, None, 5000, None, 0,
                                 None), -2, "n_wave_t"),
+    # The pointer arguments below are placeholders (256): each call is refused on the host
+    # before any of them is used.
+    (lambda h: h.rubix_cube_fwd_noalloc(*[256] * 4, 6, 221, 1221, 256, 3721, *[256] * 4, 3, 2,
+                                        256, 256, 22500, 1_000_000_000, None, 0, 0, 256, 3721,
+                                        None), -3, "static array"),
+    # the same argument checks, hence the same codes, as rubix_cube_fwd
+    (lambda h: h.rubix_cube_fwd_noalloc(*[256] * 4, 6, 221, 1221, 256, 3721, *[256] * 4, 3, 2,
+                                        256, 256, 22500, 1 << 31, None, 0, 0, 256, 3721, None),
+     -2, "bad n"),
     (lambda h: h.rubix_cube_fwd_noalloc(None, None, None, None, 6, 221, 1221, None, 3721, None,
-                                        None, None, None, 3, 2, None, None, 22500,
-                                        1_000_000_000, None, 0, 0, None, 3721, None), -3,
-     "static array"),
+                                        None, None, None, 3, 2, None, None, 22500, 10, None, 0,
+                                        0, None, 3721, None), -1, "null pointer"),
+    (lambda h: h.rubix_cube_fwd(None, None, None, None, 6, 221, 1221, None, 3721, None, None,
+                                None, None, 3, 2, None, None, 22500, 10, None, 0, 0, None, 3721,
+                                None, 0, None), -1, "null pointer"),
+    (lambda h: h.rubix_cube_noalloc_status(None, None), -1, "null pointer"),
     (lambda h: h.rubix_cube_fwd_dust(None, None, None, None, 6, 221, 1221, None, 3721, None,
                                      None, None, None, 3, 2, None, None, None, None, 22500, 10,
                                      None, 0, 0, None, 3721, None, 0, None), -1,
