@@ -45,7 +45,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "cube_fwd_ifu.txt")
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -55,7 +54,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="ifu")
+    ap.add_argument("--workload", default="large")
     ap.add_argument("--particles", type=int, default=None, help="override particle count")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -110,12 +109,18 @@ def flops_per_particle_lambda(w):
     return 7.4 + 11.0 * n_e / float(w.wave_t.size)
 
 
-def _profile_per_launch(n_particles, total_key, fixed_key):
-    """A per-launch count of the main kernel from the committed ncu summary (fixed part +
-    per-particle part), scaled to the particle count of this run."""
+def profile_file(workload):
+    """The committed ncu summary of the main kernel on this workload's spaxel grid."""
+    return os.path.join(ROOT, "profiles", f"cube_fwd_{workload}.txt")
+
+
+def _profile_per_launch(n_particles, total_key, fixed_key, workload="ifu"):
+    """A per-launch count of the main kernel from the committed ncu summary of the
+    workload (fixed part + per-particle part), scaled to the particle count of this run;
+    None when no summary exists for the workload's grid."""
     try:
         vals = {}
-        with open(TRAFFIC_FILE) as f:
+        with open(profile_file(workload)) as f:
             for line in f:
                 if ":" in line and not line.startswith("#"):
                     k, v = line.split(":", 1)
@@ -128,15 +133,15 @@ def _profile_per_launch(n_particles, total_key, fixed_key):
         return None
 
 
-def traffic_per_launch(n_particles):
+def traffic_per_launch(n_particles, workload="ifu"):
     """DRAM bytes per rubix_cube_fwd main-kernel launch (ncu, scaled to the run)."""
-    return _profile_per_launch(n_particles, "dram_bytes_per_launch", "fixed_bytes")
+    return _profile_per_launch(n_particles, "dram_bytes_per_launch", "fixed_bytes", workload)
 
 
-def instructions_per_launch(n_particles):
+def instructions_per_launch(n_particles, workload="ifu"):
     """Warp instructions per main-kernel launch (ncu smsp__inst_executed.sum, scaled)."""
     return _profile_per_launch(n_particles, "warp_instructions_per_launch",
-                               "fixed_warp_instructions")
+                               "fixed_warp_instructions", workload)
 
 
 class ClockSampler:
@@ -196,7 +201,7 @@ def dist_info():
     return world, rank, local
 
 
-# ------------------------------------------------------------------ reference arm
+# ------------------------------------------------------------------ CPU legs (oracle port)
 def _oracle_chunk(args):
     """Worker: oracle spectra of one particle chunk, summed per spaxel (float64)."""
     import oracle
@@ -210,7 +215,8 @@ def _oracle_chunk(args):
 
 
 def run_oracle_sample(w, n_sample, pool=None, chunk=256):
-    """Time the oracle port on the first n_sample particles; returns seconds."""
+    """Time the oracle port's per-particle spectra and per-spaxel sums on the first
+    n_sample particles (on `pool` when given); returns (seconds, particles kept)."""
     import oracle
 
     p = w.particles
@@ -229,7 +235,54 @@ def run_oracle_sample(w, n_sample, pool=None, chunk=256):
     for uniq, part in res:
         for u, row in zip(uniq, part):
             cube_rows[u] = cube_rows.get(u, 0.0) + row
-    return time.perf_counter() - t0, n_sample
+    return time.perf_counter() - t0, int(sel.size)
+
+
+def cpu_step_estimate(w, pool, n_sample, n_sort=2_000_000, n_planes=32, n_rows=512):
+    """One forward step of the workload on the host with the oracle port, estimated from
+    bounded samples of each stage, each scaled to the whole workload:
+      * aperture mask + spaxel assignment + stable sort of the first n_sort particles
+        (single process), scaled by N / n_sort;
+      * per-particle spectra + per-spaxel sums of n_sample particles on `pool`, scaled by
+        the workload's kept particles / the sample's;
+      * the PSF (FFT 'same' convolution per wavelength plane) of n_planes planes of the
+        full spatial field, scaled by L / n_planes;
+      * the LSF of n_rows spaxel spectra, scaled by spaxels / n_rows.
+    Returns (seconds per step, {stage: seconds})."""
+    import oracle
+
+    p = w.particles
+    N, L, S = p.n, int(w.wave_t.size), int(w.sbin)
+    ns = min(n_sort, N)
+    t0 = time.perf_counter()
+    m = oracle.mask_particles_outside_aperture(p.coords[:ns], w.edges)
+    idx = oracle.square_spaxel_assignment(p.coords[:ns], w.edges)
+    np.argsort(np.where(m, idx, S * S), kind="stable")
+    t_sort = (time.perf_counter() - t0) * N / ns
+    kept_frac = float(np.mean(m)) if ns else 1.0
+    dt, kept = run_oracle_sample(w, n_sample, pool)
+    t_part = dt * (kept_frac * N) / max(kept, 1)
+    rng = np.random.default_rng(0)
+    slab = rng.random((S, S, n_planes))
+    K = oracle.gaussian_kernel_2d(w.psf_size, w.psf_size, w.psf_sigma)
+    t0 = time.perf_counter()
+    oracle.apply_psf(slab, K, method="fft")
+    t_psf = (time.perf_counter() - t0) * L / n_planes
+    rows = rng.random((min(n_rows, S * S), L))
+    t0 = time.perf_counter()
+    oracle.apply_lsf(rows, w.lsf_sigma, w.wave_res)
+    t_lsf = (time.perf_counter() - t0) * S * S / rows.shape[0]
+    parts = {"assign_sort_s": t_sort, "spectra_and_sum_s": t_part, "psf_s": t_psf,
+             "lsf_s": t_lsf}
+    return sum(parts.values()), parts
+
+
+def cpu_sample_text(w, n_sample, cores):
+    return (f"estimated {w.name} forward step from bounded samples, each scaled to the "
+            f"workload: mask + assignment + stable sort of min(N, 2e6) particles (1 "
+            f"process), spectra + per-spaxel sums of {n_sample} particles ({cores} spawn "
+            f"processes, float64 NumPy restatement, oracle/), PSF of 32 wavelength planes "
+            f"and LSF of 512 spaxel spectra (1 process, float64)")
 
 
 def reference_arm(args):
@@ -241,18 +294,18 @@ def reference_arm(args):
     from rubix_gb300 import synth
 
     w = synth.make_workload(args.workload, n=args.particles, edge_cases=False)
-    L = w.wave_t.size
+    N, L = w.particles.n, w.wave_t.size
     cores = os.cpu_count() or 1
-    n_sample = 8192 * cores // 4
+    n_sample = 2048 * cores
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         for _ in range(args.warmup):
-            run_oracle_sample(w, min(n_sample, 4096), pool)
-        times = []
+            run_oracle_sample(w, min(n_sample, 1024), pool)
+        times, parts = [], None
         for _ in range(args.steps):
-            dt, ns = run_oracle_sample(w, n_sample, pool)
-            times.append(dt)
-    value = n_sample * L * len(times) / sum(times)
+            t, parts = cpu_step_estimate(w, pool, n_sample)
+            times.append(t)
+    value = N * L * len(times) / sum(times)
     unit = "particle*lambda/s"
     line = {
         "impl": "reference", "metric": "particles*lambda/s, particle->IFU datacube forward",
@@ -261,11 +314,12 @@ def reference_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": workload_config(w),
         "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port",
-                         "sample": f"{n_sample} particles x {L} wavelengths per step "
-                                   "(float64 NumPy restatement, spawn process pool)"},
+                         "sample": cpu_sample_text(w, n_sample, cores), "stages_s": parts},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's JAX pipeline is not installable here; this arm times the "
-                "NumPy restatement of its algorithm (oracle/) on the host cores",
+                "NumPy restatement of its algorithm (oracle/) on the host cores; the "
+                "reference design itself materialises N x L spectra (rubix/core/ifu.py:"
+                "278-283), %.0f GB for this workload" % (4.0 * N * L / 1e9),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -424,7 +478,7 @@ def dusty_bench(dev, w, d_in, steps, warmup, flush, n_gas=500_000):
             "value": N * L / (ms * 1e-3), "unit": "particle*lambda/s", "ms_per_step": ms,
             "assign_sort_av_ms": av_ms, "dusty_accumulate_ms": acc_ms,
             "gpu_launches_per_step": launches,
-            "workload": f"ifu stars ({N}) + {n_gas} gas cells (exponential disk, h_z 0.15 "
+            "workload": f"{w.name} stars ({N}) + {n_gas} gas cells (exponential disk, h_z 0.15 "
                         "kpc, log-normal masses, 12+log(O/H) 7.9-9.2), Cardelli89 R_V 3.1, "
                         "broken power-law dust-to-gas ratio (X_CO = Z)"}
 
@@ -538,6 +592,10 @@ def noise_bench(dev, cube, steps, warmup, flush):
     work = cube.clone()
     flux = ops.flux_image(work)
     med = ops.noise_median(flux)
+    if float(med) == 0.0:
+        # rubix's median is NaN (-> 0, no noise) when a spaxel is empty; time the pass
+        # with the median of the non-empty spaxels instead
+        med = flux[flux > 0].median().reshape(())
     kernel_ms = _time_steps(lambda: ops.apply_noise_(work, 20.0, "normal", 1, flux=flux,
                                                      median=med), steps, warmup, flush)
     step_ms = _time_steps(lambda: ops.apply_noise_(work, 20.0, "normal", 1), steps, warmup,
@@ -683,11 +741,82 @@ def plain_fwd_bwd_bench(dev, steps, warmup):
             "value": N * L / (ms * 1e-3), "unit": "particle*lambda/s", "ms_per_step": ms}
 
 
+def plain_assign(coords, edges, S):
+    """rubix's square_spaxel_assignment and aperture mask in stock torch operations
+    (searchsorted digitize, clip, flatten; inclusive aperture; ids >= S^2 dropped)."""
+    import torch
+
+    nb = edges.numel() - 1
+    x, y = coords[:, 0].contiguous(), coords[:, 1].contiguous()
+    ix = torch.clamp(torch.searchsorted(edges, x, right=True) - 1, 0, nb - 1)
+    iy = torch.clamp(torch.searchsorted(edges, y, right=True) - 1, 0, nb - 1)
+    idx = ix + nb * iy
+    keep = ((x >= edges[0]) & (x <= edges[-1]) & (y >= edges[0]) & (y <= edges[-1])
+            & (idx < S * S))
+    return idx, keep
+
+
+def _plain_taps(psf_sigma, psf_size, lsf_sigma, wave_res, dev):
+    """Normalised PSF and LSF taps as differentiable torch functions of the sigmas."""
+    import torch
+
+    x = torch.tensor(np.arange(-((psf_size - 1) / 2), ((psf_size - 1) / 2) + 1),
+                     dtype=torch.float32, device=dev)
+    xl = torch.tensor(np.arange(-12 * wave_res, 12 * wave_res + wave_res, wave_res,
+                                dtype=np.float32), dtype=torch.float32, device=dev)
+    e = torch.exp(-x ** 2 / (2 * psf_sigma ** 2))
+    gl = torch.exp(-0.5 * xl ** 2 / lsf_sigma ** 2)
+    return e / e.sum(), gl / gl.sum()
+
+
+def plain_galaxy_forward(r, c, v, m, z, a, edges, S, psf_sigma, psf_size, lsf_sigma,
+                         wave_res):
+    """One galaxy through the plain GPU path (stock torch operations, no kernel of
+    this package)."""
+    import torch
+
+    idx, keep = plain_assign(c, edges, S)
+    pt, lt = _plain_taps(torch.tensor(psf_sigma, device=c.device),
+                         psf_size, torch.tensor(lsf_sigma, device=c.device), wave_res,
+                         c.device)
+    return plain_cube(r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t, m, z,
+                      a, v[:, 2], idx, keep, S * S, pt, lt)
+
+
+def plain_galaxy_forward_backward(r, c, v, m, z, a, edges, S, psf_sigma, psf_size, lsf_sigma,
+                                  wave_res, target, weight, chunk=65536):
+    """Loss sum(weight (cube - target)^2) of one galaxy and its gradients (mass,
+    metallicity, age, v_los, sigma_PSF, sigma_LSF) through torch autograd of the plain
+    path.  The cube is linear in the particles and the convolutions, so the backward
+    recomputes it chunk by chunk against the cube adjoint (the whole galaxy's autograd
+    graph would not fit in memory for 10^6 particles)."""
+    import torch
+
+    idx, keep = plain_assign(c, edges, S)
+    leaves = [t.detach().clone().requires_grad_() for t in (m, z, a, v[:, 2])]
+    sp = torch.tensor(float(psf_sigma), device=c.device, requires_grad=True)
+    sl = torch.tensor(float(lsf_sigma), device=c.device, requires_grad=True)
+    grid = (r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t)
+    with torch.no_grad():
+        pt, lt = _plain_taps(sp, psf_size, sl, wave_res, c.device)
+        cube = plain_cube(*grid, *leaves, idx, keep, S * S, pt, lt)
+        d = cube - target
+        loss = (weight * d * d).sum()
+        g = 2.0 * weight * d
+    for s in range(0, c.shape[0], chunk):
+        e = min(c.shape[0], s + chunk)
+        pt, lt = _plain_taps(sp, psf_size, sl, wave_res, c.device)
+        part = plain_cube(*grid, *(x[s:e] for x in leaves), idx[s:e], keep[s:e], S * S, pt, lt)
+        (part * g).sum().backward()
+    return loss, [x.grad for x in leaves], sp.grad, sl.grad
+
+
 def ragged_bench(dev, steps, warmup):
     """256 galaxies (particle counts log-uniform 1e3-1e6, spaxel grids 16^2-64^2, PSF sigma
     0.8-2.0) rendered as one ragged batch (one launch per kernel; fwd+bwd replayed from a
-    CUDA graph; work items autotuned) and galaxy by galaxy with the single-galaxy
-    launches."""
+    CUDA graph; work items autotuned), against two per-galaxy loops: the plain GPU path
+    (stock torch operations, the loop a user of the reference's design would write on a
+    GPU) and this package's own single-galaxy launches."""
     import torch
 
     from rubix_gb300 import autotune, ragged, synth
@@ -713,6 +842,19 @@ def ragged_bench(dev, steps, warmup):
                              repeats=1)
     fwd_ms = _time_steps(lambda: b.render(*args), steps, warmup)
     loop_fwd_ms = _time_steps(lambda: ragged.render_per_galaxy(b, *args), steps, 1)
+    d_edges = [torch.from_numpy(e).to(dev) for e in edges]
+
+    def galaxy(g):
+        p0, p1 = int(b.t.poff[g]), int(b.t.poff[g + 1])
+        return [x[p0:p1] for x in args]
+
+    def plain_loop():
+        with torch.no_grad():
+            for g in range(n_gal):
+                plain_galaxy_forward(r, *galaxy(g), d_edges[g], int(sbins[g]), float(sig[g]),
+                                     int(sizes[g]), synth.LSF_SIGMA, synth.WAVE_RES)
+
+    plain_fwd_ms = _time_steps(plain_loop, 1, 0)
     with torch.no_grad():
         c0 = b.render(*args)
         target = (c0 * 1.05).contiguous()
@@ -724,10 +866,41 @@ def ragged_bench(dev, steps, warmup):
     torch.cuda.empty_cache()
     loop_fb_ms = _time_steps(
         lambda: ragged.forward_backward_per_galaxy(b, *args, target, weight), 1, 1)
+
+    # forward + backward of the plain path on a subset (every 16th galaxy), against a
+    # ragged batch of the same subset replayed from its own CUDA graph
+    sub = np.arange(0, n_gal, 16)
+    sub_b = ragged.RaggedBatch(r, counts[sub], sbins[sub], [edges[g] for g in sub], sig[sub],
+                               sizes[sub], synth.LSF_SIGMA, synth.WAVE_RES)
+    sub_args = tuple(torch.cat([galaxy(g)[k] for g in sub]) for k in range(5))
+    sub_t = torch.cat([target[int(b.t.seg_base[g]):int(b.t.seg_base[g + 1])] for g in sub])
+    sub_w = torch.cat([weight[int(b.t.seg_base[g]):int(b.t.seg_base[g + 1])] for g in sub])
+
+    def plain_sub_fb():
+        for g in sub:
+            s0, s1 = int(b.t.seg_base[g]), int(b.t.seg_base[g + 1])
+            S = int(sbins[g])
+            plain_galaxy_forward_backward(
+                r, *galaxy(g), d_edges[g], S, float(sig[g]), int(sizes[g]), synth.LSF_SIGMA,
+                synth.WAVE_RES, target[s0:s1].view(S, S, -1), weight[s0:s1].view(S, S, -1))
+
+    plain_sub_fb_ms = _time_steps(plain_sub_fb, 1, 1)
+    g_sub, _ = sub_b.capture(sub_b.forward_backward, *sub_args, sub_t, sub_w, False, warmup=1)
+    sub_fb_ms = _time_steps(g_sub.replay, steps, 1)
+    del g_sub
+    torch.cuda.empty_cache()
     autotune.set_tuning(dev.index or 0, None)
     return {"metric": "ragged mocks/s (galaxies rendered per second)",
             "fwd_value": n_gal / (fwd_ms * 1e-3), "fwd_bwd_value": n_gal / (fb_ms * 1e-3),
             "unit": "galaxies/s", "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms,
+            "plain_gpu_loop_fwd_ms": plain_fwd_ms,
+            "speedup_fwd_vs_plain_gpu_loop": plain_fwd_ms / fwd_ms,
+            "subset_fwd_bwd": {
+                "galaxies": int(sub.size), "particles": int(counts[sub].sum()),
+                "plain_gpu_loop_ms": plain_sub_fb_ms, "ragged_graph_ms": sub_fb_ms,
+                "speedup_vs_plain_gpu_loop": plain_sub_fb_ms / sub_fb_ms,
+                "plain_path": "torch autograd of the plain path, per galaxy, the backward "
+                              "recomputed per chunk of 65536 particles"},
             "per_galaxy_loop_fwd_ms": loop_fwd_ms, "per_galaxy_loop_fwd_bwd_ms": loop_fb_ms,
             "speedup_fwd": loop_fwd_ms / fwd_ms, "speedup_fwd_bwd": loop_fb_ms / fb_ms,
             "autotune": {"best_chunk_big_item": list(tune["best"]),
@@ -735,6 +908,74 @@ def ragged_bench(dev, steps, warmup):
             "batch": f"{n_gal} galaxies, {int(counts.sum())} particles, "
                      f"{b.n_segments} spaxels x {b.L} wavelengths, PSF sigma 0.8-2.0 "
                      f"(kernels up to {b.m}x{b.m}), LSF sigma {synth.LSF_SIGMA} A"}
+
+
+def ifu_bench(dev, steps, warmup, flush):
+    """The 10^6-particle IFU workload (150 x 150 x 3721 cube): the same forward step as
+    the main line (device time, inputs resident, L2 flushed) and the fused accumulate
+    launch inside it."""
+    import torch
+
+    from rubix_gb300 import synth
+    from rubix_gb300.api import IFURenderer
+
+    w = synth.make_workload("ifu", edge_cases=False)
+    p = w.particles
+    rnd = IFURenderer.from_workload(w, device=dev)
+    d_in = [torch.from_numpy(a).to(dev) for a in (p.coords, p.velocity, p.mass, p.metallicity,
+                                                   p.age)]
+    acc = []
+
+    def step():
+        idx, mask = rnd.assign(d_in[0])
+        perm, offs = rnd.sort(idx, mask)
+        e0, e1 = _events()
+        e0.record()
+        cube = rnd.accumulate(d_in[2], d_in[3], d_in[4], d_in[1], perm, offs, with_lsf=True)
+        e1.record()
+        acc.append((e0, e1))
+        return rnd.noise_(rnd.psf(cube))
+
+    ms = _time_steps(step, steps, warmup, flush)
+    torch.cuda.synchronize()
+    acc_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in acc[-steps:])
+    N, L = p.n, int(w.wave_t.size)
+    return {"metric": "particles*lambda/s, particle->IFU datacube forward",
+            "value": N * L / (ms * 1e-3), "unit": "particle*lambda/s", "ms_per_step": ms,
+            "accumulate_ms": acc_ms, "workload": workload_config(w)["workload"]}
+
+
+def summary_block(line):
+    """The headline figures of the line in one short object, printed last (so that the
+    end of the line, which log tails keep, carries them)."""
+    def get(*keys):
+        d = line
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    return {
+        "workload": (get("config", "workload") or "").split(":")[0],
+        "value": get("value"), "ms_per_step": get("ms_per_step"),
+        "e2e_value": get("e2e", "value"), "e2e_ms_per_step": get("e2e", "ms_per_step"),
+        "accumulate_ms": get("roofline", "ms_per_launch"),
+        "accumulate_hbm_frac": get("roofline", "frac"),
+        "accumulate_issue_frac": get("roofline", "issue", "frac"),
+        "step_hbm_frac": get("roofline", "step", "frac"),
+        "cpu_baseline_value": get("cpu_baseline", "value"),
+        "ifu_ms_per_step": get("ifu", "ms_per_step"),
+        "fwd_bwd_over_fwd": get("fwd_bwd", "fwd_bwd_over_fwd"),
+        "ours_over_plain_gpu": get("plain_gpu", "ours_over_plain"),
+        "fwd_bwd_ours_over_plain_gpu": get("plain_gpu_fwd_bwd", "ours_over_plain"),
+        "ragged_fwd_vs_plain_gpu_loop": get("ragged", "speedup_fwd_vs_plain_gpu_loop"),
+        "ragged_fwd_bwd_vs_plain_gpu_loop": get("ragged", "subset_fwd_bwd",
+                                                "speedup_vs_plain_gpu_loop"),
+        "ragged_fwd_vs_own_kernel_loop": get("ragged", "speedup_fwd"),
+        "ragged_fwd_bwd_vs_own_kernel_loop": get("ragged", "speedup_fwd_bwd"),
+        "psf_ms": get("psf", "ms"),
+    }
 
 
 # ------------------------------------------------------------------ our arm
@@ -882,7 +1123,7 @@ def main():
     alg_bytes = 20 * N + flux_bytes + S2 * L * 4   # particle fields + perm, SSP flux, cube write
     cube_avg_s = statistics.mean(cube_ms) * 1e-3
     achieved = alg_bytes / cube_avg_s / 1e9
-    traffic = traffic_per_launch(N)
+    traffic = traffic_per_launch(N, w.name)
     fpl = flops_per_particle_lambda(w)
     fp32_peak = fp32_peak_tflops(dev)
     fp32_achieved = fpl * N * L / cube_avg_s / 1e12
@@ -893,7 +1134,7 @@ def main():
     # instruction issue, the resource the main kernel is bound by: warp instructions per
     # launch (ncu count, scaled to N) over the launch time, against one instruction per
     # cycle per scheduler (4 per SM) at the SM clock sampled during the timed region
-    insts = instructions_per_launch(N) if not dusty else None  # profile: dust-free kernel
+    insts = instructions_per_launch(N, w.name) if not dusty else None  # dust-free kernel
     issue = None
     if insts:
         sm_mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
@@ -901,7 +1142,7 @@ def main():
         peak_issue = n_sm * 4 * sm_mhz * 1e6
         issue = {"warp_instructions_per_launch": insts, "achieved_per_s": insts / cube_avg_s,
                  "peak_per_s": peak_issue, "frac": insts / cube_avg_s / peak_issue,
-                 "source": "smsp__inst_executed.sum of profiles/cube_fwd_ifu.txt scaled to "
+                 "source": f"smsp__inst_executed.sum of profiles/cube_fwd_{w.name}.txt scaled to "
                            f"{N} particles; peak = {n_sm} SMs x 4 schedulers x 1 warp "
                            f"instruction per cycle at {sm_mhz:.0f} MHz"}
     roofline = {"kernel": "rubix_cube_fwd (fused lookup/mass/Doppler/resample/accumulate)",
@@ -911,22 +1152,39 @@ def main():
                 "ms_per_launch": statistics.mean(cube_ms),
                 "share_of_step": statistics.mean(cube_ms) / statistics.mean(step_ms),
                 "fp32": compute}
+    # the whole step against the path's algorithmic traffic 24 N + |T| + 5 C (particle
+    # fields read once, SSP flux once, cube written by the accumulate, PSF read + write,
+    # LSF read + write)
+    step_bytes = 24 * N + flux_bytes + 5 * S2 * L * 4
+    step_gbs = step_bytes / (statistics.mean(step_ms) * 1e-3) / 1e9
+    roofline["step"] = {"algorithmic_bytes": step_bytes, "achieved": step_gbs, "peak": peak,
+                        "unit": "GB/s", "frac": step_gbs / peak,
+                        "ms_per_step": statistics.mean(step_ms)}
 
-    # ---------------- CPU baseline (rank 0, N=1): oracle port, one core, bounded sample
+    # ---------------- CPU baseline (rank 0, N=1): oracle port on the host cores, an
+    # estimated step from bounded samples of every stage
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        n_sample = 1024
-        run_oracle_sample(w, 128)
-        dt, ns = run_oracle_sample(w, n_sample)
-        cpu = {"value": ns * L / dt, "unit": "particle*lambda/s", "cores": 1, "kind": "port",
-               "sample": f"first {ns} particles of the workload x {L} wavelengths, float64 "
-                         "NumPy restatement (oracle/), single process"}
+        import multiprocessing as mp
+
+        cores = os.cpu_count() or 1
+        n_sample = 2048 * cores
+        with mp.get_context("spawn").Pool(cores) as pool:
+            run_oracle_sample(w, 512, pool)
+            t_cpu, parts = cpu_step_estimate(w, pool, n_sample)
+        cpu = {"value": N * L / t_cpu, "unit": "particle*lambda/s", "cores": cores,
+               "kind": "port", "sample": cpu_sample_text(w, n_sample, cores),
+               "ms_per_step": 1e3 * t_cpu, "stages_s": parts,
+               "reference_design": "rubix materialises the N x L resampled spectra "
+                                   "(rubix/core/ifu.py:278-283): %.0f GB for this workload"
+                                   % (4.0 * N * L / 1e9)}
 
     # ---------------- fwd+bwd, plain GPU path and ragged batch (rank 0, N=1)
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
         ours_final = step_device()
         for name, fn in (
+                ("ifu", lambda: ifu_bench(dev, args.steps, 3, flush)),
                 ("fwd_bwd", lambda: fwd_bwd_bench(dev, min(args.steps, 5), 3, flush)),
                 ("plain_gpu", lambda: plain_bench(dev, w, rnd, d_in, ours_final, args.steps,
                                                   args.warmup, flush)),
@@ -968,6 +1226,7 @@ def main():
             "gpu_launches": launches, "clocks": clocks, "wall_s_timed": wall,
         }
         line.update(extras)
+        line["summary"] = summary_block(line)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

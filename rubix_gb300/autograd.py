@@ -163,12 +163,16 @@ class DatacubeFunction(torch.autograd.Function):
 
 
 def render_cube(renderer, coords, velocity, mass, metallicity, age, sigma_psf, sigma_lsf,
-                psf_size: int, wave_res: float, gas=None):
+                psf_size: int, wave_res: float, gas=None, log_age: bool = False):
     """Differentiable datacube of one galaxy: aperture filter, spaxel sort (no
     gradient) and ``DatacubeFunction``.  All particle tensors must be CUDA tensors;
     ``sigma_psf`` / ``sigma_lsf`` are tensors (or floats when no gradient is wanted).
     ``gas`` = (coords, mass, metals) with a renderer built with ``dust`` applies the dust
-    extinction (A_V computed once, without gradient)."""
+    extinction (A_V computed once, without gradient).  With ``log_age`` the ``age``
+    tensor holds log10(age / Gyr): the SSP lookup receives 10^age (float32) and the
+    gradient is dL/dlog10(age) = dL/dage * age * ln 10."""
+    if log_age:
+        age = torch.pow(10.0, age)
     idx, mask = renderer.assign(coords)
     perm, offs = renderer.sort(idx, mask)
     av = None
