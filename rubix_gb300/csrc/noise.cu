@@ -140,6 +140,14 @@ __global__ void __launch_bounds__(1024) select_block_kernel(const float* __restr
   __shared__ int s_bad;
   __shared__ unsigned s_res[2];
   const int tid = threadIdx.x;
+  // rubix's median is NaN (hence 0) as soon as one value is <= 0 (or NaN): one pass
+  // over the values settles that before any histogram pass
+  int bad0 = 0;
+  for (long long i = tid; i < n; i += blockDim.x) bad0 |= !(v[i] > 0.f);
+  if (__syncthreads_or(bad0) || n == 0) {
+    if (tid == 0) *median = 0.f;
+    return;
+  }
   if (tid == 0) s_bad = 0;
   for (int which = 0; which < 2; ++which) {
     if (tid == 0) {
@@ -231,6 +239,9 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_kernel(
     const float* __restrict__ flux, const float* __restrict__ median, float inv_s2n,
     int distribution, uint32_t k0, uint32_t k1, int vec) {
   const float scale = sqrtf(*median) * inv_s2n;
+  // a zero median (rubix's rule for a cube with an empty spaxel) adds no noise: every
+  // finite element stays as it is, so the pass is skipped
+  if (!(scale != 0.f)) return;
   for (long long s = blockIdx.x; s < n_spaxels; s += gridDim.x) {
     const float f = flux[s];
     const float sig = f > 0.f ? scale / sqrtf(f) : 0.f;
