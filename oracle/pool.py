@@ -26,17 +26,19 @@ def _init(ssp_metallicity, ssp_age, ssp_flux, wave_z, wave_t):
 
 
 def _sum_job(job):
-    """Sum of the float64 resampled, mass-scaled spectra of one block of particles
-    (the per-spaxel segment sum of calculate_cube, rubix/spectra/ifu.py:270-288)."""
-    mass, met, age, vz = job
+    """Per-group sums of the float64 resampled, mass-scaled spectra of one block of
+    particles (the per-spaxel segment sum of calculate_cube, rubix/spectra/ifu.py:
+    270-288); returns (group ids, sums)."""
+    gid, mass, met, age, vz = job
     g = _GRID
-    tot = np.zeros(g["wave_t"].size)
+    uniq, inv = np.unique(gid, return_inverse=True)
+    tot = np.zeros((uniq.size, g["wave_t"].size))
     for s in range(0, mass.size, 512):
         sp = particle_spectra(mass[s:s + 512], met[s:s + 512], age[s:s + 512], vz[s:s + 512],
                               g["ssp_metallicity"], g["ssp_age"], g["ssp_flux"], g["wave_z"],
                               g["wave_t"])
-        tot += sp.sum(axis=0)
-    return tot
+        np.add.at(tot, inv[s:s + 512], sp)
+    return uniq, tot
 
 
 def spaxel_spectra(groups, ssp_metallicity, ssp_age, ssp_flux, wave_z, wave_t,
@@ -45,17 +47,19 @@ def spaxel_spectra(groups, ssp_metallicity, ssp_age, ssp_flux, wave_z, wave_t,
 
     ``groups``: list of (mass, metallicity, age, v_los) arrays, one tuple per spaxel
     (the particles assigned to it, filter_particles already applied).  Returns an
-    (n_groups, L) float64 array.  Each group is cut into blocks of ``block`` particles
-    that run in parallel on ``processes`` workers (default: every host core)."""
+    (n_groups, L) float64 array.  The particles of all groups, in group order, are cut
+    into blocks of ``block`` that run in parallel on ``processes`` workers (default:
+    every host core); a block may hold many small groups or part of a large one."""
     L = np.asarray(wave_t).size
-    jobs, owner = [], []
-    for gi, (m, z, a, v) in enumerate(groups):
-        for s in range(0, m.size, block):
-            jobs.append((m[s:s + block], z[s:s + block], a[s:s + block], v[s:s + block]))
-            owner.append(gi)
     out = np.zeros((len(groups), L))
-    if not jobs:
+    sizes = np.array([np.size(gr[0]) for gr in groups], dtype=np.int64)
+    if sizes.sum() == 0:
         return out
+    gid = np.repeat(np.arange(len(groups)), sizes)
+    cols = [np.concatenate([np.asarray(gr[k], dtype=np.float32) for gr in groups])
+            for k in range(4)]
+    jobs = [(gid[s:s + block], *(c[s:s + block] for c in cols))
+            for s in range(0, gid.size, block)]
     n_proc = max(1, min(processes or os.cpu_count() or 1, len(jobs)))
     grid = (np.asarray(ssp_metallicity), np.asarray(ssp_age), np.asarray(ssp_flux),
             np.asarray(wave_z), np.asarray(wave_t))
@@ -66,6 +70,6 @@ def spaxel_spectra(groups, ssp_metallicity, ssp_age, ssp_flux, wave_z, wave_t,
         ctx = mp.get_context("spawn")
         with ctx.Pool(n_proc, initializer=_init, initargs=grid) as pool:
             res = pool.map(_sum_job, jobs, chunksize=1)
-    for gi, r in zip(owner, res):
-        out[gi] += r
+    for uniq, tot in res:
+        out[uniq] += tot
     return out
