@@ -187,6 +187,26 @@ RUBIX_API int rubix_cube_bwd_dust(const float* ssp_flux, const float* ssp_metall
                                   void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * rubix_cube_bwd_dust plus grad_av[i] = dL/dA_V of every particle (the derivative of its
+ * transmission 2^(ext_exponent[t] * av[i]) in its spectrum), which jax.grad through
+ * calculate_extinction (rubix/core/dust.py:53-63) passes on to the column density.
+ * Same workspace and limits as rubix_cube_bwd.
+ */
+RUBIX_API int rubix_cube_bwd_dust_av(const float* ssp_flux, const float* ssp_metallicity,
+                                     const float* ssp_age, const float* ssp_wave_z,
+                                     int32_t n_met, int32_t n_age, int32_t n_wave,
+                                     const float* wave_t, int32_t n_wave_t, const float* mass,
+                                     const float* metallicity, const float* age,
+                                     const float* velocity, int64_t vel_stride,
+                                     int32_t vel_component, const float* av,
+                                     const float* ext_exponent, const int32_t* perm,
+                                     const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                     const float* adj, int64_t adj_stride, float* grad_mass,
+                                     float* grad_metallicity, float* grad_age, float* grad_vlos,
+                                     float* grad_av, void* workspace, size_t workspace_bytes,
+                                     void* stream);
+
+/*
  * Replaces the per-cell extinction of rubix/spectra/dust/dust_extinction.py:291-306
  * (12 + log10(O/(16 H)), calculate_dust_to_gas_ratio :13-90, calculate_extinction
  * :93-160, divided by the spaxel area).
@@ -232,6 +252,42 @@ RUBIX_API int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const i
                             int64_t star_stride, const int32_t* star_pa, int64_t n_stars,
                             int32_t n_segments, int32_t pa_limit, float* av_out,
                             void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * What jax.grad through rubix's column interpolation gives
+ * (rubix/spectra/dust/dust_extinction.py:262-343, the jnp.interp of each star's z on
+ * the masked cumulative extinction of its spaxel) and through the per-cell extinction
+ * (dust_extinction.py:291-306, dust-to-gas ratio of 12 + log10(O/(16 H))).
+ *
+ * rubix_dust_av_bwd: given grad_av[i] = dL/dA_V of every star, writes
+ * grad_star_z[i] = dL/dz of the star (the slope of its interpolation; 0 when clamped)
+ * and grad_gas_ext[j] = dL/d ext of every gas cell (the cumulative sums' adjoint); the
+ * gas heights are held fixed.  Same inputs and limits as rubix_dust_av; workspace
+ * rubix_dust_av_bwd_workspace_size (256-byte aligned).  Deterministic: records are
+ * sorted by node and summed in star order (float64).
+ */
+RUBIX_API size_t rubix_dust_av_bwd_workspace_size(int64_t n_gas, int32_t n_segments,
+                                                  int64_t n_stars);
+RUBIX_API int rubix_dust_av_bwd(const float* gas_coords, int64_t gas_stride,
+                                const int32_t* gas_pa, const float* gas_ext, int64_t n_gas,
+                                const float* star_coords, int64_t star_stride,
+                                const int32_t* star_pa, int64_t n_stars, int32_t n_segments,
+                                int32_t pa_limit, const float* grad_av, float* grad_star_z,
+                                float* grad_gas_ext, void* workspace, size_t workspace_bytes,
+                                void* stream);
+
+/*
+ * The adjoint of rubix_dust_gas_extinction: from grad_ext[j] = dL/d ext of each cell,
+ * grad_mass[j] = dL/d mass, grad_h[j] = dL/d metals[j][h_col] and grad_o[j] = dL/d
+ * metals[j][o_col] (the other metal columns do not enter).  Same parameters as the
+ * forward.
+ */
+RUBIX_API int rubix_dust_gas_extinction_bwd(const float* mass, const float* metals,
+                                            int64_t metals_stride, int32_t h_col,
+                                            int32_t o_col, int64_t n, const float* dgr_params,
+                                            int32_t broken, float scale, float spaxel_area,
+                                            const float* grad_ext, float* grad_mass,
+                                            float* grad_h, float* grad_o, void* stream);
 
 /*
  * Replaces the array preparation of rubix/core/fits.py:88-100 (astropy writing

@@ -240,20 +240,21 @@ def extinguish(ax, Av):
 # Dust mass and per-cell extinction: spectra/dust/dust_extinction.py:13-160
 # ----------------------------------------------------------------------------------
 
-def dust_to_gas_ratio(log_oh, model, Xco):
+def dust_to_gas_ratio(log_oh, model, Xco, dtype=np.float32):
     """calculate_dust_to_gas_ratio (dust_extinction.py:13-90), Remy-Ruyer et al. 2014
-    Table 1, float32."""
-    g = np.asarray(log_oh, np.float32)
+    Table 1, float32 (``dtype=np.float64`` for differences)."""
+    F32 = dtype  # noqa: N806 -- the arithmetic type of this evaluation
+    g = np.asarray(log_oh, dtype)
     x_sol = F32(8.69)
     if model == "power law slope fixed":
         raise NotImplementedError("power law slope fixed not implemented yet.")
     if Xco == "MW":
         if model == "power law slope free":
-            return (F32(1) / F32(10) ** (F32(2.21) + F32(1.62) * (x_sol - g))).astype(np.float32)
+            return (F32(1) / F32(10) ** (F32(2.21) + F32(1.62) * (x_sol - g))).astype(dtype)
         a, ah, b, al, xt = 2.21, 1.00, 0.68, 3.08, 7.96
     elif Xco == "Z":
         if model == "power law slope free":
-            return (F32(1) / F32(10) ** (F32(2.21) + F32(2.02) * (x_sol - g))).astype(np.float32)
+            return (F32(1) / F32(10) ** (F32(2.21) + F32(2.02) * (x_sol - g))).astype(dtype)
         a, ah, b, al, xt = 2.21, 1.00, 0.96, 3.10, 8.10
     else:
         raise ValueError(f"unknown Xco {Xco!r}")
@@ -261,14 +262,14 @@ def dust_to_gas_ratio(log_oh, model, Xco):
         raise ValueError(f"unknown dust_to_gas_model {model!r}")
     hi = F32(10) ** (F32(a) + F32(ah) * (x_sol - g))
     lo = F32(10) ** (F32(b) + F32(al) * (x_sol - g))
-    return (F32(1) / np.where(g > F32(xt), hi, lo)).astype(np.float32)
+    return (F32(1) / np.where(g > F32(xt), hi, lo)).astype(dtype)
 
 
-def log_oh(metals, h_col=0, o_col=4):
+def log_oh(metals, h_col=0, o_col=4, dtype=np.float32):
     """12 + log10(O / (16 H)) of every gas cell (dust_extinction.py:291-293)."""
-    m = np.asarray(metals, np.float32)
+    m = np.asarray(metals, dtype)
     with np.errstate(all="ignore"):
-        return (F32(12) + np.log10(m[:, o_col] / (F32(16) * m[:, h_col]))).astype(np.float32)
+        return (dtype(12) + np.log10(m[:, o_col] / (dtype(16) * m[:, h_col]))).astype(dtype)
 
 
 def extinction_scale(dust_grain_density, effective_wavelength=5448.0):
@@ -279,17 +280,19 @@ def extinction_scale(dust_grain_density, effective_wavelength=5448.0):
                                   * dust_grain_density)
 
 
-def gas_extinction(mass, metals, spaxel_area, dust=None, h_col=0, o_col=4):
+def gas_extinction(mass, metals, spaxel_area, dust=None, h_col=0, o_col=4,
+                   dtype=np.float32):
     """Per-cell extinction of the gas: dust mass (gas mass times the dust-to-gas ratio
     of 12 + log(O/H)) through calculate_extinction, divided by the spaxel area
-    (dust_extinction.py:291-306), float32."""
+    (dust_extinction.py:291-306), float32 (``dtype=np.float64`` for differences)."""
     d = dict(DUST_DEFAULTS)
     d.update(dust or {})
-    dgr = dust_to_gas_ratio(log_oh(metals, h_col, o_col), d["dust_to_gas_model"], d["Xco"])
-    dm = (np.asarray(mass, np.float32) * dgr).astype(np.float32)
+    dgr = dust_to_gas_ratio(log_oh(metals, h_col, o_col, dtype), d["dust_to_gas_model"],
+                            d["Xco"], dtype)
+    dm = (np.asarray(mass, dtype) * dgr).astype(dtype)
     with np.errstate(all="ignore"):
-        e = (dm * F32(extinction_scale(d["dust_grain_density"]))).astype(np.float32)
-        return (e / F32(spaxel_area)).astype(np.float32)
+        e = (dm * dtype(extinction_scale(d["dust_grain_density"]))).astype(dtype)
+        return (e / dtype(spaxel_area)).astype(dtype)
 
 
 # ----------------------------------------------------------------------------------
@@ -299,28 +302,29 @@ def gas_extinction(mass, metals, spaxel_area, dust=None, h_col=0, o_col=4):
 _INTERP_EPS = np.spacing(np.finfo(np.float32).eps)
 
 
-def jax_interp(x, xp, fp, left_extrapolate=True):
-    """``jnp.interp(x, xp, fp, left="extrapolate")`` in float32: bracket
+def jax_interp(x, xp, fp, left_extrapolate=True, dtype=np.float32):
+    """``jnp.interp(x, xp, fp, left="extrapolate")`` in float32 (or ``dtype``): bracket
     i = clip(searchsorted(xp, x, 'right'), 1, n-1), fp[i-1] + (x - xp[i-1]) / dx * df
     (fp[i-1] where |dx| <= spacing(eps)), fp[-1] to the right of xp[-1]."""
-    x = np.asarray(x, np.float32)
-    xp = np.asarray(xp, np.float32)
-    fp = np.asarray(fp, np.float32)
+    x = np.asarray(x, dtype)
+    xp = np.asarray(xp, dtype)
+    fp = np.asarray(fp, dtype)
     i = np.clip(np.searchsorted(xp, x, side="right"), 1, len(xp) - 1)
-    df = (fp[i] - fp[i - 1]).astype(np.float32)
-    dx = (xp[i] - xp[i - 1]).astype(np.float32)
-    delta = (x - xp[i - 1]).astype(np.float32)
+    df = (fp[i] - fp[i - 1]).astype(dtype)
+    dx = (xp[i] - xp[i - 1]).astype(dtype)
+    delta = (x - xp[i - 1]).astype(dtype)
     dx0 = np.abs(dx) <= _INTERP_EPS
     with np.errstate(all="ignore"):
-        q = (delta / np.where(dx0, F32(1), dx)).astype(np.float32)
-        f = np.where(dx0, fp[i - 1], (fp[i - 1] + (q * df).astype(np.float32)).astype(np.float32))
+        q = (delta / np.where(dx0, dtype(1), dx)).astype(dtype)
+        f = np.where(dx0, fp[i - 1], (fp[i - 1] + (q * df).astype(dtype)).astype(dtype))
     if not left_extrapolate:
         f = np.where(x < xp[0], fp[0], f)
     f = np.where(x > xp[-1], fp[-1], f)
-    return f.astype(np.float32)
+    return f.astype(dtype)
 
 
-def spaxel_av(gas_z, gas_pa, gas_ext, star_z, star_pa, n_spaxels, spaxels=None):
+def spaxel_av(gas_z, gas_pa, gas_ext, star_z, star_pa, n_spaxels, spaxels=None,
+              dtype=np.float32):
     """Av of every star (dust_extinction.py:262-343), step by step.
 
     Gas and stars are lexsorted by (pixel assignment, z); for each spaxel the gas
@@ -329,12 +333,13 @@ def spaxel_av(gas_z, gas_pa, gas_ext, star_z, star_pa, n_spaxels, spaxels=None):
     pairs are sorted stably and the spaxel's stars take ``jnp.interp`` of their z with
     left extrapolation.  ``spaxels`` restricts the loop to those spaxel ids (the Av of
     stars of other spaxels is then left at 0) so large inputs can be spot-checked.
-    Returns float32 Av in the input order of the stars.
+    Returns float32 Av in the input order of the stars (``dtype=np.float64``: the same
+    steps in float64, for differences; the gas heights are then taken as given).
     """
-    gz = np.asarray(gas_z, np.float32)
+    gz = np.asarray(gas_z, dtype)
     gpa = np.asarray(gas_pa, np.int64)
-    gext = np.asarray(gas_ext, np.float32)
-    sz = np.asarray(star_z, np.float32)
+    gext = np.asarray(gas_ext, dtype)
+    sz = np.asarray(star_z, dtype)
     spa = np.asarray(star_pa, np.int64)
     ng, ns = gz.size, sz.size
     gsi = np.lexsort((gz, gpa))
@@ -345,24 +350,24 @@ def spaxel_av(gas_z, gas_pa, gas_ext, star_z, star_pa, n_spaxels, spaxels=None):
     ext_sorted = gext[gsi]
     z_sorted = gz[gsi]
     sz_sorted = sz[ssi]
-    big = F32(1e30)
+    big = dtype(1e30) if dtype is np.float64 else F32(1e30)
     pos_g = np.arange(ng)
-    av = np.zeros(ns, np.float32)
+    av = np.zeros(ns, dtype)
     loop = ids if spaxels is None else np.asarray(spaxels, np.int64)
     for idx in loop:
         s0, s1 = sb[idx], sb[idx + 1]
         if s1 <= s0 or ng == 0:
             continue
         gmask = (pos_g >= gb[idx]) & (pos_g < gb[idx + 1])
-        gmask2 = np.where(gmask, F32(1), big).astype(np.float32)
+        gmask2 = np.where(gmask, dtype(1), big).astype(dtype)
         with np.errstate(invalid="ignore"):
-            cum = (np.cumsum((ext_sorted * gmask).astype(np.float32), dtype=np.float32)
-                   * gmask).astype(np.float32)
-            xp = (z_sorted * gmask2).astype(np.float32)
+            cum = (np.cumsum((ext_sorted * gmask).astype(dtype), dtype=dtype)
+                   * gmask).astype(dtype)
+            xp = (z_sorted * gmask2).astype(dtype)
         order = np.argsort(xp, kind="stable")
         xp, fp = xp[order], cum[order]
         # only the spaxel's own stars keep their value (star_mask)
-        av[s0:s1] += jax_interp(sz_sorted[s0:s1], xp, fp, left_extrapolate=True)
+        av[s0:s1] += jax_interp(sz_sorted[s0:s1], xp, fp, left_extrapolate=True, dtype=dtype)
     out = np.empty_like(av)
     out[ssi] = av
     return out

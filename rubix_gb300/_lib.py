@@ -101,6 +101,20 @@ SIGNATURES = {
          _vp, _i64, _vp, _vp, _vp, _vp,
          _vp, _sz, _vp],
     ),
+    "rubix_cube_bwd_dust_av": (
+        _c.c_int,
+        [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32,
+         _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp,
+         _vp, _vp, _i32, _i64,
+         _vp, _i64, _vp, _vp, _vp, _vp, _vp,
+         _vp, _sz, _vp],
+    ),
+    "rubix_dust_av_bwd_workspace_size": (_sz, [_i64, _i32, _i64]),
+    "rubix_dust_av_bwd": (_c.c_int, [_vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _i32,
+                                     _i32, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "rubix_dust_gas_extinction_bwd": (_c.c_int, [_vp, _vp, _i64, _i32, _i32, _i64, _vp, _i32,
+                                                 _c.c_float, _c.c_float, _vp, _vp, _vp, _vp,
+                                                 _vp]),
     "rubix_ragged_assign": (_c.c_int, [_vp, _i64, _i64, _vp, _i32, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _vp]),
     "rubix_ragged_psf_fwd": (_c.c_int, [_vp, _vp, _i32, _i64, _i64, _i32, _vp, _vp, _vp, _i32,

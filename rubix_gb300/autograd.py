@@ -136,12 +136,17 @@ class DatacubeFunction(torch.autograd.Function):
         gP = ops.psf_forward(g, rtp)
         need = ctx.needs_input_grad
         grads = [None] * 12
-        if any(need[:4]):
+        want_av = len(need) > 11 and need[11]
+        if any(need[:4]) or want_av:
             h = ops.lsf_forward(gP, rtl, len(tl) - 1 - crop)
-            gm, gz, ga, gv = ops.cube_backward(
+            out = ops.cube_backward(
                 r.ssp_flux, r.ssp_metallicity, r.ssp_age, r.ssp_wave_z, r.wave_t, mass,
                 metallicity, age, velocity, r.velocity_axis, ctx.perm, ctx.seg_offsets, nseg,
-                h.view(nseg, -1), dust_av=ctx.dust[0], dust_exponent=ctx.dust[1])
+                h.view(nseg, -1), dust_av=ctx.dust[0], dust_exponent=ctx.dust[1],
+                av_grad=want_av)
+            gm, gz, ga, gv = out[:4]
+            if want_av:
+                grads[11] = out[4].view_as(ctx.dust[0]).to(ctx.dust[0].dtype)
             grads[0] = gm.view_as(mass).to(mass.dtype) if need[0] else None
             grads[1] = gz.view_as(metallicity).to(metallicity.dtype) if need[1] else None
             grads[2] = ga.view_as(age).to(age.dtype) if need[2] else None
@@ -162,13 +167,66 @@ class DatacubeFunction(torch.autograd.Function):
         return tuple(grads)
 
 
+class DustColumnFunction(torch.autograd.Function):
+    """A_V [n_stars] of every star from the gas in front of it (rubix's
+    calculate_extinction: the dust mass of each gas cell from its mass and 12 +
+    log10(O/H), cells outside the aperture emptied, the cumulative column of the star's
+    spaxel interpolated at the star's z; rubix/core/dust.py:16-65,
+    rubix/spectra/dust/dust_extinction.py:169-343) as a differentiable function of the
+    stars' coordinates (z: the x and y pick the spaxel, a piecewise-constant choice, and
+    get no gradient, as in rubix) and of the gas masses and metal fractions (hydrogen and
+    oxygen columns).  The gas coordinates are held fixed.  ``star_idx`` are the stars'
+    spaxel assignments; ``renderer`` an ``IFURenderer`` built with ``dust``."""
+
+    @staticmethod
+    def forward(ctx, star_coords, gas_mass, gas_metals, renderer, star_idx, gas_coords):
+        r = renderer
+        gc = gas_coords.contiguous()
+        gidx = ops.spaxel_assign(gc, r.edges)
+        gm = gas_mass.contiguous()
+        keep = None
+        if r.apply_filter:
+            keep = ops.aperture_mask(gc, r.edges)
+            gm = ops.mask_zero_(gm.clone(), keep)
+        gext = ops.dust_gas_extinction(gm, gas_metals, r.dgr_params, r.dgr_broken,
+                                       r.ext_scale, r.spaxel_area)
+        nb = int(r.edges.numel()) - 1
+        nseg = r.sbin * r.sbin
+        pa_limit = max(nb * nb, nseg)
+        av = ops.dust_av(gc, gidx, gext, star_coords, star_idx, nseg, pa_limit)
+        ctx.save_for_backward(star_coords, gm, gas_metals, gc, gidx, gext, star_idx)
+        ctx.keep = keep
+        ctx.r, ctx.nseg, ctx.pa_limit = r, nseg, pa_limit
+        return av
+
+    @staticmethod
+    def backward(ctx, g):
+        star_coords, gm, gas_metals, gc, gidx, gext, star_idx = ctx.saved_tensors
+        r = ctx.r
+        gz, gdext = ops.dust_av_backward(gc, gidx, gext, star_coords, star_idx, ctx.nseg,
+                                         ctx.pa_limit, g.contiguous().float())
+        g_coords = None
+        if ctx.needs_input_grad[0]:
+            g_coords = torch.zeros_like(star_coords)
+            g_coords.view(-1, 3)[:, 2] = gz
+        g_mass = g_met = None
+        if ctx.needs_input_grad[1] or ctx.needs_input_grad[2]:
+            g_mass, g_met = ops.dust_gas_extinction_backward(
+                gm, gas_metals, r.dgr_params, r.dgr_broken, r.ext_scale, r.spaxel_area, gdext)
+            if ctx.keep is not None:
+                g_mass = ops.mask_zero_(g_mass, ctx.keep)  # emptied cells: no dependence
+        return (g_coords, g_mass if ctx.needs_input_grad[1] else None,
+                g_met if ctx.needs_input_grad[2] else None, None, None, None)
+
+
 def render_cube(renderer, coords, velocity, mass, metallicity, age, sigma_psf, sigma_lsf,
                 psf_size: int, wave_res: float, gas=None, log_age: bool = False):
     """Differentiable datacube of one galaxy: aperture filter, spaxel sort (no
     gradient) and ``DatacubeFunction``.  All particle tensors must be CUDA tensors;
     ``sigma_psf`` / ``sigma_lsf`` are tensors (or floats when no gradient is wanted).
     ``gas`` = (coords, mass, metals) with a renderer built with ``dust`` applies the dust
-    extinction (A_V computed once, without gradient).  With ``log_age`` the ``age``
+    extinction; gradients reach A_V and through it the stars' z and the gas masses and
+    metal fractions (``DustColumnFunction``) when those require them.  With ``log_age`` the ``age``
     tensor holds log10(age / Gyr): the SSP lookup receives 10^age (float32) and the
     gradient is dL/dlog10(age) = dL/dage * age * ln 10."""
     if log_age:
@@ -177,7 +235,11 @@ def render_cube(renderer, coords, velocity, mass, metallicity, age, sigma_psf, s
     perm, offs = renderer.sort(idx, mask)
     av = None
     if gas is not None:
-        with torch.no_grad():
-            av = renderer.dust_av(coords, idx, *gas)
+        if torch.is_grad_enabled() and (coords.requires_grad or gas[1].requires_grad
+                                        or gas[2].requires_grad):
+            av = DustColumnFunction.apply(coords, gas[1], gas[2], renderer, idx, gas[0])
+        else:
+            with torch.no_grad():
+                av = renderer.dust_av(coords, idx, *gas)
     return DatacubeFunction.apply(mass, metallicity, age, velocity, sigma_psf, sigma_lsf,
                                   renderer, perm, offs, psf_size, wave_res, av)

@@ -49,6 +49,7 @@ struct AdjArgs {
   float* g_met;
   float* g_age;
   float* g_vlos;
+  float* g_av;  // dust only: dL/dA_V per particle (optional)
   CubeCtrl* ctrl;
   const int2* bucket;
   int row_cap;
@@ -182,7 +183,9 @@ __device__ __forceinline__ void walk_step2(float x, unsigned& aa, unsigned& ab, 
 
 // The 8 partial sums of one particle over this thread's R wavelengths.  With kDust the
 // cube adjoint h_t is seen through the particle's dust transmission 2^(e_t A_V): the
-// particle adds beta g_t I_t to the cube, so every sum against h takes h_t g_t.
+// particle adds beta g_t I_t to the cube, so every sum against h takes h_t g_t; `sav`
+// then also takes sum_t h_t g_t e_t I_t, the A_V derivative of the particle's term up to
+// beta ln 2 (d 2^(e A_V) / dA_V = ln 2 e 2^(e A_V)).
 template <int R, bool kGeneric, bool kDust>
 __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
                                          const float4* __restrict__ rb, int ks, int ke, float B,
@@ -190,7 +193,7 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
                                          const float (&lam)[R], const float (&dlam)[R],
                                          const float (&h)[R], float (&s)[kAdjSums],
                                          const float* __restrict__ e2, float av, int t0,
-                                         int n_t) {
+                                         int n_t, float& sav) {
   const float u = A0 - B;
   int b = __float_as_int(u + 12582912.0f) - 0x4B400000;
   b = min(max(b, 0), kBuckets - 1);
@@ -208,6 +211,7 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
   unsigned ab = static_cast<unsigned>(__cvta_generic_to_shared(rb + k));
 #pragma unroll
   for (int i = 0; i < kAdjSums; ++i) s[i] = 0.f;
+  sav = 0.f;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const float x = lam[r];
@@ -223,7 +227,11 @@ __device__ __forceinline__ void adj_eval(const float4* __restrict__ ra,
     const float IZ = fmaf(d, f.y, f.x);
     const float IA = fmaf(d, f.w, f.z);
     float hr = h[r];
-    if constexpr (kDust) hr = __fmul_rn(hr, dust_transmission(__ldg(e2 + min(t0 + r, n_t - 1)), av));
+    if constexpr (kDust) {
+      const float er = __ldg(e2 + min(t0 + r, n_t - 1));
+      hr = __fmul_rn(hr, dust_transmission(er, av));
+      sav = fmaf(__fmul_rn(hr, er), I, sav);
+    }
     s[0] = fmaf(hr, I, s[0]);
     s[1] = fmaf(dlam[r], I, s[1]);
     s[2] = fmaf(hr, IZ, s[2]);
@@ -279,6 +287,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
   __shared__ uint64_t s_bar;
   __shared__ int s_item, s_fail;
   __shared__ float4 s_wt[2][2];  // mixing / derivative weights of the current, next particle
+  __shared__ float s_red_av[2][kAdjWarps];  // dust: the A_V sum of each warp
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (a.staged)
@@ -359,17 +368,23 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
       const int4 rb = rec.b;
       const int ks = rb.y, ke = rb.z & ~kGenericFlag;
       float sums[kAdjSums];
+      float sav = 0.f;
       const float av = kDust ? rec.c.w : 0.f;
       if (rb.z & kGenericFlag)
         adj_eval<R, true, kDust>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam, dlam,
-                                 h, sums, a.dust_e2, av, t0, n_t);
+                                 h, sums, a.dust_e2, av, t0, n_t, sav);
       else
         adj_eval<R, false, kDust>(s_ra - ks, s_rb - ks, ks, ke, rec.a.z, A0, s_bucket, lam,
-                                  dlam, h, sums, a.dust_e2, av, t0, n_t);
+                                  dlam, h, sums, a.dust_e2, av, t0, n_t, sav);
       const float wv = warp_reduce8(sums, lane);
       if ((lane & 3) == 0) {
         const int v = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
         s_red[(buf * kAdjWarps + warp) * kAdjSums + v] = wv;
+      }
+      if constexpr (kDust) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sav += __shfl_xor_sync(0xffffffffu, sav, o);
+        if (lane == 0) s_red_av[buf][warp] = sav;
       }
       __syncthreads();  // partial sums visible; rows free for the next particle
       if (warp == 0) {
@@ -392,9 +407,16 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
         if (lane == 0) {
           const float m = rec.a.x, T = rec.c.x, TZ = rec.c.y, TA = rec.c.z;
           const float sc = T / Tp;
-          float gm = 0.f, gz = 0.f, ga = 0.f, gv = 0.f;
+          float gm = 0.f, gz = 0.f, ga = 0.f, gv = 0.f, gav = 0.f;
           if (Tp != 0.f && isfinite(sc)) {
             const float beta = m * sc;
+            if constexpr (kDust) {
+              if (a.g_av) {
+                float t = 0.f;  // the warps' A_V sums in warp order
+                for (int w = 0; w < kAdjWarps; ++w) t += s_red_av[buf][w];
+                gav = beta * 0.69314718055994531f * t;
+              }
+            }
             const float k = m / Tp;
             const float inv_c = (float)(1.0 / kSpeedOfLight);
             gm = sc * gamma;
@@ -410,6 +432,7 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
           if (a.g_met) a.g_met[i] = gz;
           if (a.g_age) a.g_age[i] = ga;
           if (a.g_vlos) a.g_vlos[i] = gv;
+          if (kDust && a.g_av) a.g_av[i] = gav;
         }
       }
     }
@@ -465,7 +488,7 @@ int cube_bwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
                   const float* dust_e2, const int32_t* perm, const int32_t* seg_offsets,
                   int32_t n_segments, int64_t n, const float* adj, int64_t adj_stride,
                   float* grad_mass, float* grad_metallicity, float* grad_age, float* grad_vlos,
-                  void* workspace, size_t workspace_bytes, void* stream) {
+                  float* grad_av, void* workspace, size_t workspace_bytes, void* stream) {
   RUBIX_REQUIRE(n >= 0 && n < (1LL << 31), RUBIX_E_SHAPE, "%s: bad n", who);
   RUBIX_REQUIRE(n_segments >= 0, RUBIX_E_SHAPE, "%s: n_segments < 0", who);
   RUBIX_REQUIRE(n_met >= 2 && n_age >= 2, RUBIX_E_SHAPE,
@@ -478,7 +501,7 @@ int cube_bwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
                 "%s: vel_component outside the velocity row", who);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // every gradient entry is written: zeros for particles outside the sorted set
-  float* grads[4] = {grad_mass, grad_metallicity, grad_age, grad_vlos};
+  float* grads[5] = {grad_mass, grad_metallicity, grad_age, grad_vlos, grad_av};
   for (float* g : grads)
     if (g && n > 0) RUBIX_CUDA_TRY(cudaMemsetAsync(g, 0, sizeof(float) * (size_t)n, st));
   if (n_segments == 0 || n == 0) return RUBIX_OK;
@@ -531,6 +554,7 @@ int cube_bwd_impl(const char* who, const float* ssp_flux, const float* ssp_metal
   args.g_met = grad_metallicity;
   args.g_age = grad_age;
   args.g_vlos = grad_vlos;
+  args.g_av = grad_av;
   args.ctrl = L.ctrl;
   args.bucket = L.bucket;
   args.row_cap = row_cap;
@@ -565,7 +589,7 @@ extern "C" int rubix_cube_bwd(const float* ssp_flux, const float* ssp_metallicit
                        n_age, n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity,
                        vel_stride, vel_component, nullptr, nullptr, perm, seg_offsets,
                        n_segments, n, adj, adj_stride, grad_mass, grad_metallicity, grad_age,
-                       grad_vlos, workspace, workspace_bytes, stream);
+                       grad_vlos, nullptr, workspace, workspace_bytes, stream);
 }
 
 extern "C" int rubix_cube_bwd_dust(const float* ssp_flux, const float* ssp_metallicity,
@@ -585,5 +609,27 @@ extern "C" int rubix_cube_bwd_dust(const float* ssp_flux, const float* ssp_metal
                        n_met, n_age, n_wave, wave_t, n_wave_t, mass, metallicity, age, velocity,
                        vel_stride, vel_component, av, ext_exponent, perm, seg_offsets,
                        n_segments, n, adj, adj_stride, grad_mass, grad_metallicity, grad_age,
-                       grad_vlos, workspace, workspace_bytes, stream);
+                       grad_vlos, nullptr, workspace, workspace_bytes, stream);
+}
+
+extern "C" int rubix_cube_bwd_dust_av(const float* ssp_flux, const float* ssp_metallicity,
+                                      const float* ssp_age, const float* ssp_wave_z,
+                                      int32_t n_met, int32_t n_age, int32_t n_wave,
+                                      const float* wave_t, int32_t n_wave_t, const float* mass,
+                                      const float* metallicity, const float* age,
+                                      const float* velocity, int64_t vel_stride,
+                                      int32_t vel_component, const float* av,
+                                      const float* ext_exponent, const int32_t* perm,
+                                      const int32_t* seg_offsets, int32_t n_segments, int64_t n,
+                                      const float* adj, int64_t adj_stride, float* grad_mass,
+                                      float* grad_metallicity, float* grad_age,
+                                      float* grad_vlos, float* grad_av, void* workspace,
+                                      size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(ext_exponent != nullptr && (n == 0 || av != nullptr), RUBIX_E_INVALID,
+                "rubix_cube_bwd_dust_av: null A_V or extinction exponent");
+  return cube_bwd_impl("rubix_cube_bwd_dust_av", ssp_flux, ssp_metallicity, ssp_age,
+                       ssp_wave_z, n_met, n_age, n_wave, wave_t, n_wave_t, mass, metallicity,
+                       age, velocity, vel_stride, vel_component, av, ext_exponent, perm,
+                       seg_offsets, n_segments, n, adj, adj_stride, grad_mass, grad_metallicity,
+                       grad_age, grad_vlos, grad_av, workspace, workspace_bytes, stream);
 }

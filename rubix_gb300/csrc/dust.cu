@@ -218,6 +218,7 @@ struct Node {
   float x, f;
   int p;  // P position (tie order)
   bool ok;
+  bool own;  // a cell of the star's own spaxel (its value is a cumulative sum)
 };
 
 __device__ __forceinline__ bool node_before(const Node& a, const Node& b) {
@@ -225,13 +226,15 @@ __device__ __forceinline__ bool node_before(const Node& a, const Node& b) {
 }
 
 __device__ __forceinline__ Node own_node(const DustView& v, int q) {
-  return Node{v.nz[q], v.nf[q], v.np_[q], true};
+  return Node{v.nz[q], v.nf[q], v.np_[q], true, true};
 }
 
 __device__ __forceinline__ Node other_node(const DustView& v, int k) {
-  if (k < 0 || k >= v.ng) return Node{0.f, 0.f, 0, false};
-  return Node{v.gk[k], 0.f, v.gp[k], true};
+  if (k < 0 || k >= v.ng) return Node{0.f, 0.f, 0, false, false};
+  return Node{v.gk[k], 0.f, v.gp[k], true, false};
 }
+
+__device__ __forceinline__ Node no_node() { return Node{0.f, 0.f, 0, false, false}; }
 
 // First G index >= k outside segment s (ng if none); last G index <= k outside s (-1).
 __device__ __forceinline__ int other_next(const DustView& v, int k, int s) {
@@ -262,74 +265,249 @@ __device__ __forceinline__ float interp_pair(const Node& L, const Node& R, float
   return __fadd_rn(L.f, __fmul_rn(__fdiv_rn(delta, dx), df));
 }
 
+// How a star's A_V follows from the merged nodes of its spaxel.
+enum StarMode { kNoGas = 0, kLast = 1, kFlat = 2, kInterp = 3 };
+
+struct StarInterp {
+  Node A, B, last;
+  int mode;  // kNoGas: 0; kLast: last.f (one node, or right of every node); kFlat: A.f
+             // (a pair closer than float32 spacing); kInterp: A.f + (x - A.x)/dx * df
+};
+
+// The nodes of one star at height x in spaxel s (jnp.interp with left extrapolation
+// on rubix's merged (key, value) pairs, the pairs formed only where needed).
+__device__ __forceinline__ StarInterp star_interp(const DustView& v, float x, int s) {
+  StarInterp r;
+  r.A = r.B = r.last = no_node();
+  r.mode = kNoGas;
+  if (v.ng == 0) return r;
+  const int ob = v.seg_off[s], oe = v.seg_off[s + 1];
+  // last node of the merged order (right clamp) and the single-node case
+  Node last = oe > ob ? own_node(v, oe - 1) : no_node();
+  {
+    const Node t = other_node(v, other_prev(v, v.ng - 1, s));
+    if (t.ok && (!last.ok || node_before(last, t))) last = t;
+  }
+  r.last = last;
+  if (v.ng == 1) {
+    r.mode = kLast;
+    return r;
+  }
+  const int qo = upper_bound(v.nz, ob, oe, x);  // own nodes <= x: [ob, qo)
+  const int kg = upper_bound(v.gk, 0, v.ng, x);  // G entries <= x: [0, kg)
+  Node L = qo > ob ? own_node(v, qo - 1) : no_node();
+  Node R = qo < oe ? own_node(v, qo) : no_node();
+  {
+    const Node t = other_node(v, other_prev(v, kg - 1, s));
+    if (t.ok && (!L.ok || node_before(L, t))) L = t;
+    const Node u = other_node(v, other_next(v, kg, s));
+    if (u.ok && (!R.ok || node_before(u, R))) R = u;
+  }
+  Node A, B;
+  if (!L.ok) {
+    // x below every node: the first two nodes (left extrapolation)
+    const Node o0 = ob < oe ? own_node(v, ob) : no_node();
+    const Node o1 = ob + 1 < oe ? own_node(v, ob + 1) : no_node();
+    const int g0 = other_next(v, 0, s);
+    const Node t0 = other_node(v, g0);
+    const Node t1 = other_node(v, other_next(v, g0 + 1, s));
+    if (o0.ok && (!t0.ok || node_before(o0, t0))) {
+      A = o0;
+      B = (o1.ok && (!t0.ok || node_before(o1, t0))) ? o1 : t0;
+    } else {
+      A = t0;
+      B = (o0.ok && (!t1.ok || node_before(o0, t1))) ? o0 : t1;
+    }
+  } else if (!R.ok) {
+    // x at or above every node: the last two nodes
+    const Node o1 = oe > ob ? own_node(v, oe - 1) : no_node();
+    const Node o0 = oe - 1 > ob ? own_node(v, oe - 2) : no_node();
+    const int g1 = other_prev(v, v.ng - 1, s);
+    const Node t1 = other_node(v, g1);
+    const Node t0 = other_node(v, other_prev(v, g1 - 1, s));
+    if (o1.ok && (!t1.ok || node_before(t1, o1))) {
+      B = o1;
+      A = (o0.ok && (!t1.ok || node_before(t1, o0))) ? o0 : t1;
+    } else {
+      B = t1;
+      A = (o1.ok && (!t0.ok || node_before(t0, o1))) ? o1 : t0;
+    }
+  } else {
+    A = L;
+    B = R;
+  }
+  r.A = A;
+  r.B = B;
+  if (x > last.x)
+    r.mode = kLast;
+  else
+    r.mode = fabsf(__fsub_rn(B.x, A.x)) <= 1.4210855e-14f ? kFlat : kInterp;
+  return r;
+}
+
 __global__ void dust_star_av_kernel(DustView v, const float* __restrict__ coords,
                                     long long stride, const int* __restrict__ pa, long long n,
                                     float* __restrict__ av) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    if (v.ng == 0) {
-      av[i] = 0.f;
-      continue;
-    }
     const float x = coords[i * stride + 2];
     const int s = min(max(pa[i], 0), v.nseg - 1);
-    const int ob = v.seg_off[s], oe = v.seg_off[s + 1];
-    // last node of the merged order (right clamp) and the single-node case
-    Node last = oe > ob ? own_node(v, oe - 1) : Node{0.f, 0.f, 0, false};
-    {
-      const Node t = other_node(v, other_prev(v, v.ng - 1, s));
-      if (t.ok && (!last.ok || node_before(last, t))) last = t;
-    }
-    if (v.ng == 1) {
-      av[i] = last.f;
-      continue;
-    }
-    const int qo = upper_bound(v.nz, ob, oe, x);  // own nodes <= x: [ob, qo)
-    const int kg = upper_bound(v.gk, 0, v.ng, x);  // G entries <= x: [0, kg)
-    Node L = qo > ob ? own_node(v, qo - 1) : Node{0.f, 0.f, 0, false};
-    Node R = qo < oe ? own_node(v, qo) : Node{0.f, 0.f, 0, false};
-    {
-      const Node t = other_node(v, other_prev(v, kg - 1, s));
-      if (t.ok && (!L.ok || node_before(L, t))) L = t;
-      const Node u = other_node(v, other_next(v, kg, s));
-      if (u.ok && (!R.ok || node_before(u, R))) R = u;
-    }
-    Node A, B;
-    if (!L.ok) {
-      // x below every node: the first two nodes (left extrapolation)
-      const Node o0 = ob < oe ? own_node(v, ob) : Node{0.f, 0.f, 0, false};
-      const Node o1 = ob + 1 < oe ? own_node(v, ob + 1) : Node{0.f, 0.f, 0, false};
-      const int g0 = other_next(v, 0, s);
-      const Node t0 = other_node(v, g0);
-      const Node t1 = other_node(v, other_next(v, g0 + 1, s));
-      if (o0.ok && (!t0.ok || node_before(o0, t0))) {
-        A = o0;
-        B = (o1.ok && (!t0.ok || node_before(o1, t0))) ? o1 : t0;
-      } else {
-        A = t0;
-        B = (o0.ok && (!t1.ok || node_before(o0, t1))) ? o0 : t1;
-      }
-    } else if (!R.ok) {
-      // x at or above every node: the last two nodes
-      const Node o1 = oe > ob ? own_node(v, oe - 1) : Node{0.f, 0.f, 0, false};
-      const Node o0 = oe - 1 > ob ? own_node(v, oe - 2) : Node{0.f, 0.f, 0, false};
-      const int g1 = other_prev(v, v.ng - 1, s);
-      const Node t1 = other_node(v, g1);
-      const Node t0 = other_node(v, other_prev(v, g1 - 1, s));
-      if (o1.ok && (!t1.ok || node_before(t1, o1))) {
-        B = o1;
-        A = (o0.ok && (!t1.ok || node_before(t1, o0))) ? o0 : t1;
-      } else {
-        B = t1;
-        A = (o1.ok && (!t0.ok || node_before(t0, o1))) ? o1 : t0;
-      }
-    } else {
-      A = L;
-      B = R;
-    }
-    float f = interp_pair(A, B, x);
-    if (x > last.x) f = last.f;
+    const StarInterp r = star_interp(v, x, s);
+    float f = 0.f;
+    if (r.mode == kLast)
+      f = r.last.f;
+    else if (r.mode != kNoGas)
+      f = interp_pair(r.A, r.B, x);
     av[i] = f;
+  }
+}
+
+// Adjoint of dust_star_av_kernel for an upstream gradient g_i = dL/dA_V,i.  A_V is
+// a_A f_A + a_B f_B of (at most) two node values, f = 0 for cells of other spaxels and
+// the cumulative extinction of the spaxel's cells up to the node otherwise; its
+// derivative in the star's z is g df/dx between two nodes (the node positions, i.e.
+// the gas heights, are held fixed).  Each star emits two records (P position of the
+// node, or n_gas for a node whose value does not depend on the cells; weight) and its
+// z derivative.
+__global__ void dust_star_av_bwd_kernel(DustView v, const float* __restrict__ coords,
+                                        long long stride, const int* __restrict__ pa,
+                                        long long n, const float* __restrict__ dav,
+                                        float* __restrict__ dz, unsigned* __restrict__ rkey,
+                                        int* __restrict__ rval, float* __restrict__ rw) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float x = coords[i * stride + 2];
+    const int s = min(max(pa[i], 0), v.nseg - 1);
+    const float g = dav[i];
+    const StarInterp r = star_interp(v, x, s);
+    const unsigned none = (unsigned)v.ng;
+    unsigned ka = none, kb = none;
+    float wa = 0.f, wb = 0.f, gz = 0.f;
+    if (r.mode == kLast) {
+      if (r.last.own) { ka = (unsigned)r.last.p; wa = g; }
+    } else if (r.mode == kFlat) {
+      if (r.A.own) { ka = (unsigned)r.A.p; wa = g; }
+    } else if (r.mode == kInterp) {
+      const float dx = __fsub_rn(r.B.x, r.A.x);
+      const float q = __fdiv_rn(__fsub_rn(x, r.A.x), dx);
+      const float df = __fsub_rn(r.B.f, r.A.f);
+      gz = g * (df / dx);
+      if (r.A.own) { ka = (unsigned)r.A.p; wa = g * (1.f - q); }
+      if (r.B.own) { kb = (unsigned)r.B.p; wb = g * q; }
+    }
+    dz[i] = gz;
+    rkey[2 * i] = ka;
+    rkey[2 * i + 1] = kb;
+    rval[2 * i] = (int)(2 * i);
+    rval[2 * i + 1] = (int)(2 * i + 1);
+    rw[2 * i] = wa;
+    rw[2 * i + 1] = wb;
+  }
+}
+
+// Records sorted by node (stable): each thread sums the runs of equal keys inside its
+// tile of kRunTile records in order (float64) and writes the sum at the position where
+// the run's part in this tile begins.
+constexpr int kRunTile = 256;
+
+__global__ void dust_run_partial_kernel(const unsigned* __restrict__ key,
+                                        const int* __restrict__ val,
+                                        const float* __restrict__ w, long long n,
+                                        double* __restrict__ partial) {
+  const long long tiles = (n + kRunTile - 1) / kRunTile;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tiles;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long b = t * kRunTile, e = min(n, b + kRunTile);
+    long long start = b;
+    double sum = 0.0;
+    for (long long j = b; j < e; ++j) {
+      if (j > b && key[j] != key[j - 1]) {
+        partial[start] = sum;
+        start = j;
+        sum = 0.0;
+      }
+      sum += (double)w[val[j]];
+    }
+    partial[start] = sum;
+  }
+}
+
+// The total of every run that starts in this thread's tile: its partial there plus the
+// partials at the starts of the following tiles it reaches into, in tile order; runs
+// of key >= n_gas are dropped.  gnode[key] = total (gnode zeroed before).
+__global__ void dust_run_total_kernel(const unsigned* __restrict__ key,
+                                      const double* __restrict__ partial, long long n,
+                                      unsigned n_gas, double* __restrict__ gnode) {
+  const long long tiles = (n + kRunTile - 1) / kRunTile;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tiles;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long b = t * kRunTile, e = min(n, b + kRunTile);
+    for (long long j = b; j < e; ++j) {
+      if (j > 0 && key[j] == key[j - 1]) continue;  // not a run start
+      const unsigned k = key[j];
+      if (k >= n_gas) continue;
+      double tot = partial[j];
+      for (long long nb = e; nb < n && key[nb] == k; nb += kRunTile) tot += partial[nb];
+      gnode[k] = tot;
+    }
+  }
+}
+
+// Per segment of the P order (one warp each), the suffix sums of the node gradients:
+// d ext_P[j] = sum over P positions q >= j of the segment of gnode[q] (cum[q] holds
+// ext_P[j] for every j <= q of the segment), written to the cell perm[j].
+__global__ void dust_suffix_kernel(const double* __restrict__ gnode,
+                                   const int* __restrict__ seg_off, int nseg,
+                                   const int* __restrict__ perm, float* __restrict__ dext) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nseg; s += warps) {
+    const int b = seg_off[s], e = seg_off[s + 1];
+    double carry = 0.0;
+    for (int top = e; top > b; top -= 32) {
+      const int j = top - 1 - lane;  // lane 0 the highest position of this chunk
+      double x = j >= b ? gnode[j] : 0.0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      x += carry;
+      if (j >= b) dext[perm[j]] = (float)x;
+      carry = __shfl_sync(0xffffffffu, x, 31);
+    }
+  }
+}
+
+// d ext / d(mass, H, O) of gas_extinction_kernel times the upstream dL/d ext:
+// ext = mass dgr scale / area, dgr = 10^-y, y = a + alpha (x_sol - g),
+// g = 12 + log10(O / (16 H)): d ext/d mass = dgr scale / area, d ext/dO = alpha ext / O,
+// d ext/dH = -alpha ext / H (alpha of the branch the forward took).
+__global__ void gas_extinction_bwd_kernel(const float* __restrict__ mass,
+                                          const float* __restrict__ metals, long long mstride,
+                                          int h_col, int o_col, long long n, DgrParams p,
+                                          float scale, float area,
+                                          const float* __restrict__ dext,
+                                          float* __restrict__ dmass, float* __restrict__ dh,
+                                          float* __restrict__ dox) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float h = metals[i * mstride + h_col], o = metals[i * mstride + o_col];
+    const float g = __fadd_rn(12.f, log10f(__fdiv_rn(o, __fmul_rn(16.f, h))));
+    const float d = __fsub_rn(p.x_sol, g);
+    float y = __fadd_rn(p.a_hi, __fmul_rn(p.alpha_hi, d));
+    float alpha = p.alpha_hi;
+    if (p.broken && !(g > p.x_t)) {
+      y = __fadd_rn(p.a_lo, __fmul_rn(p.alpha_lo, d));
+      alpha = p.alpha_lo;
+    }
+    const float dgr = __fdiv_rn(1.f, exp10f(y));
+    const float k = __fdiv_rn(__fmul_rn(dgr, scale), area);  // d ext / d mass
+    const float ext = __fmul_rn(mass[i], k);
+    const float gi = dext[i];
+    dmass[i] = gi * k;
+    dox[i] = gi * alpha * ext / o;
+    dh[i] = -gi * alpha * ext / h;
   }
 }
 
@@ -394,64 +572,45 @@ DustLayout carve_dust(void* base, long long ng, int nseg) {
   return L;
 }
 
+struct DustBwdLayout {
+  DustLayout fwd;
+  unsigned *rk0, *rk1;
+  int *rv0, *rv1, *rhist;
+  float* rw;
+  double *partial, *gnode;
+  size_t bytes;
+};
+
+DustBwdLayout carve_dust_bwd(void* base, long long ng, int nseg, long long ns) {
+  DustBwdLayout B;
+  B.fwd = carve_dust(base, ng, nseg);
+  Carve c(base ? static_cast<char*>(base) + B.fwd.bytes : nullptr);
+  const size_t nr = (size_t)(2 * (ns > 0 ? ns : 1));
+  B.rk0 = c.take<unsigned>(nr);
+  B.rk1 = c.take<unsigned>(nr);
+  B.rv0 = c.take<int>(nr);
+  B.rv1 = c.take<int>(nr);
+  B.rhist = c.take<int>((size_t)radix_hist_ints((long long)nr));
+  B.rw = c.take<float>(nr);
+  B.partial = c.take<double>(nr);
+  B.gnode = c.take<double>((size_t)(ng > 0 ? ng : 1));
+  B.bytes = B.fwd.bytes + c.off;
+  return B;
+}
+
 }  // namespace
 }  // namespace rubix
 
-using namespace rubix;
+namespace rubix {
+namespace {
 
-extern "C" int rubix_dust_gas_extinction(const float* mass, const float* metals,
-                                         int64_t metals_stride, int32_t h_col, int32_t o_col,
-                                         int64_t n, const float* dgr_params, int32_t broken,
-                                         float scale, float spaxel_area, float* ext_out,
-                                         void* stream) {
-  RUBIX_REQUIRE(n >= 0, RUBIX_E_INVALID, "rubix_dust_gas_extinction: n < 0");
-  RUBIX_REQUIRE(h_col >= 0 && o_col >= 0 && h_col < metals_stride && o_col < metals_stride,
-                RUBIX_E_INVALID, "rubix_dust_gas_extinction: H/O columns outside the rows");
-  RUBIX_REQUIRE(dgr_params != nullptr, RUBIX_E_INVALID,
-                "rubix_dust_gas_extinction: null dgr_params");
-  if (n == 0) return RUBIX_OK;
-  RUBIX_REQUIRE(mass && metals && ext_out, RUBIX_E_INVALID,
-                "rubix_dust_gas_extinction: null pointer");
-  DgrParams p{dgr_params[0], dgr_params[1], dgr_params[2], dgr_params[3], dgr_params[4],
-              dgr_params[5], broken};
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  gas_extinction_kernel<<<grid_for(n, 256), 256, 0, st>>>(mass, metals, metals_stride, h_col,
-                                                          o_col, n, p, scale, spaxel_area,
-                                                          ext_out);
-  RUBIX_LAUNCH_CHECK("gas_extinction_kernel");
-  return RUBIX_OK;
-}
-
-extern "C" size_t rubix_dust_av_workspace_size(int64_t n_gas, int32_t n_segments) {
-  if (n_gas < 0 || n_segments < 1) return 0;
-  return carve_dust(nullptr, n_gas, n_segments).bytes;
-}
-
-extern "C" int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const int32_t* gas_pa,
-                             const float* gas_ext, int64_t n_gas, const float* star_coords,
-                             int64_t star_stride, const int32_t* star_pa, int64_t n_stars,
-                             int32_t n_segments, int32_t pa_limit, float* av_out,
-                             void* workspace, size_t workspace_bytes, void* stream) {
-  RUBIX_REQUIRE(n_gas >= 0 && n_gas < (1LL << 31) - 1, RUBIX_E_SHAPE,
-                "rubix_dust_av: n_gas must be in [0, 2^31 - 1)");
-  RUBIX_REQUIRE(n_stars >= 0, RUBIX_E_SHAPE, "rubix_dust_av: n_stars < 0");
-  RUBIX_REQUIRE(n_segments >= 1 && pa_limit >= n_segments, RUBIX_E_SHAPE,
-                "rubix_dust_av: need 1 <= n_segments <= pa_limit");
-  RUBIX_REQUIRE(gas_stride >= 3 && star_stride >= 3, RUBIX_E_SHAPE,
-                "rubix_dust_av: coordinate rows need 3 components");
-  if (n_stars == 0) return RUBIX_OK;
-  RUBIX_REQUIRE(star_coords && star_pa && av_out, RUBIX_E_INVALID,
-                "rubix_dust_av: null star pointer");
-  RUBIX_REQUIRE(n_gas == 0 || (gas_coords && gas_pa && gas_ext), RUBIX_E_INVALID,
-                "rubix_dust_av: null gas pointer");
-  const size_t need = rubix_dust_av_workspace_size(n_gas, n_segments);
-  RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
-                "rubix_dust_av: workspace of %zu bytes needed, %zu given", need,
-                workspace_bytes);
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const DustLayout L = carve_dust(workspace, n_gas, n_segments);
+// The node structure of rubix_dust_av (P, Q and G orders, segment offsets, cumulative
+// sums) built in the layout L; v describes it to the star kernels.
+int dust_setup(const float* gas_coords, int64_t gas_stride, const int32_t* gas_pa,
+               const float* gas_ext, int64_t n_gas, int32_t n_segments, int32_t pa_limit,
+               const DustLayout& L, DustView& v, cudaStream_t st) {
   const long long ng = n_gas;
-  DustView v{};
+  v = DustView{};
   v.ng = (int)ng;
   v.nseg = n_segments;
   if (ng > 0) {
@@ -511,11 +670,165 @@ extern "C" int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const 
     v.rid = L.rid;
     v.run_start = L.run_start;
   }
+  return RUBIX_OK;
+}
+
+}  // namespace
+}  // namespace rubix
+
+using namespace rubix;
+
+extern "C" int rubix_dust_gas_extinction(const float* mass, const float* metals,
+                                         int64_t metals_stride, int32_t h_col, int32_t o_col,
+                                         int64_t n, const float* dgr_params, int32_t broken,
+                                         float scale, float spaxel_area, float* ext_out,
+                                         void* stream) {
+  RUBIX_REQUIRE(n >= 0, RUBIX_E_INVALID, "rubix_dust_gas_extinction: n < 0");
+  RUBIX_REQUIRE(h_col >= 0 && o_col >= 0 && h_col < metals_stride && o_col < metals_stride,
+                RUBIX_E_INVALID, "rubix_dust_gas_extinction: H/O columns outside the rows");
+  RUBIX_REQUIRE(dgr_params != nullptr, RUBIX_E_INVALID,
+                "rubix_dust_gas_extinction: null dgr_params");
+  if (n == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(mass && metals && ext_out, RUBIX_E_INVALID,
+                "rubix_dust_gas_extinction: null pointer");
+  DgrParams p{dgr_params[0], dgr_params[1], dgr_params[2], dgr_params[3], dgr_params[4],
+              dgr_params[5], broken};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gas_extinction_kernel<<<grid_for(n, 256), 256, 0, st>>>(mass, metals, metals_stride, h_col,
+                                                          o_col, n, p, scale, spaxel_area,
+                                                          ext_out);
+  RUBIX_LAUNCH_CHECK("gas_extinction_kernel");
+  return RUBIX_OK;
+}
+
+extern "C" size_t rubix_dust_av_workspace_size(int64_t n_gas, int32_t n_segments) {
+  if (n_gas < 0 || n_segments < 1) return 0;
+  return carve_dust(nullptr, n_gas, n_segments).bytes;
+}
+
+extern "C" int rubix_dust_av(const float* gas_coords, int64_t gas_stride, const int32_t* gas_pa,
+                             const float* gas_ext, int64_t n_gas, const float* star_coords,
+                             int64_t star_stride, const int32_t* star_pa, int64_t n_stars,
+                             int32_t n_segments, int32_t pa_limit, float* av_out,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+  RUBIX_REQUIRE(n_gas >= 0 && n_gas < (1LL << 31) - 1, RUBIX_E_SHAPE,
+                "rubix_dust_av: n_gas must be in [0, 2^31 - 1)");
+  RUBIX_REQUIRE(n_stars >= 0, RUBIX_E_SHAPE, "rubix_dust_av: n_stars < 0");
+  RUBIX_REQUIRE(n_segments >= 1 && pa_limit >= n_segments, RUBIX_E_SHAPE,
+                "rubix_dust_av: need 1 <= n_segments <= pa_limit");
+  RUBIX_REQUIRE(gas_stride >= 3 && star_stride >= 3, RUBIX_E_SHAPE,
+                "rubix_dust_av: coordinate rows need 3 components");
+  if (n_stars == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(star_coords && star_pa && av_out, RUBIX_E_INVALID,
+                "rubix_dust_av: null star pointer");
+  RUBIX_REQUIRE(n_gas == 0 || (gas_coords && gas_pa && gas_ext), RUBIX_E_INVALID,
+                "rubix_dust_av: null gas pointer");
+  const size_t need = rubix_dust_av_workspace_size(n_gas, n_segments);
+  RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
+                "rubix_dust_av: workspace of %zu bytes needed, %zu given", need,
+                workspace_bytes);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const DustLayout L = carve_dust(workspace, n_gas, n_segments);
+  DustView v{};
+  {
+    const int rc = dust_setup(gas_coords, gas_stride, gas_pa, gas_ext, n_gas, n_segments,
+                              pa_limit, L, v, st);
+    if (rc != RUBIX_OK) return rc;
+  }
   // one star per thread: the binary searches are latency-bound, so no grid cap
   const long long star_blocks = (n_stars + 255) / 256;
   dust_star_av_kernel<<<(unsigned)std::min<long long>(star_blocks, 1LL << 30), 256, 0, st>>>(
       v, star_coords, star_stride, star_pa, n_stars, av_out);
   RUBIX_LAUNCH_CHECK("dust_star_av_kernel");
+  return RUBIX_OK;
+}
+
+extern "C" size_t rubix_dust_av_bwd_workspace_size(int64_t n_gas, int32_t n_segments,
+                                                   int64_t n_stars) {
+  if (n_gas < 0 || n_segments < 1 || n_stars < 0) return 0;
+  return carve_dust_bwd(nullptr, n_gas, n_segments, n_stars).bytes;
+}
+
+extern "C" int rubix_dust_av_bwd(const float* gas_coords, int64_t gas_stride,
+                                 const int32_t* gas_pa, const float* gas_ext, int64_t n_gas,
+                                 const float* star_coords, int64_t star_stride,
+                                 const int32_t* star_pa, int64_t n_stars, int32_t n_segments,
+                                 int32_t pa_limit, const float* grad_av, float* grad_star_z,
+                                 float* grad_gas_ext, void* workspace, size_t workspace_bytes,
+                                 void* stream) {
+  RUBIX_REQUIRE(n_gas >= 0 && n_gas < (1LL << 31) - 1, RUBIX_E_SHAPE,
+                "rubix_dust_av_bwd: n_gas must be in [0, 2^31 - 1)");
+  RUBIX_REQUIRE(n_stars >= 0 && n_stars < (1LL << 30), RUBIX_E_SHAPE,
+                "rubix_dust_av_bwd: n_stars must be in [0, 2^30)");
+  RUBIX_REQUIRE(n_segments >= 1 && pa_limit >= n_segments, RUBIX_E_SHAPE,
+                "rubix_dust_av_bwd: need 1 <= n_segments <= pa_limit");
+  RUBIX_REQUIRE(gas_stride >= 3 && star_stride >= 3, RUBIX_E_SHAPE,
+                "rubix_dust_av_bwd: coordinate rows need 3 components");
+  RUBIX_REQUIRE(n_stars == 0 || (star_coords && star_pa && grad_av && grad_star_z),
+                RUBIX_E_INVALID, "rubix_dust_av_bwd: null star pointer");
+  RUBIX_REQUIRE(n_gas == 0 || (gas_coords && gas_pa && gas_ext && grad_gas_ext),
+                RUBIX_E_INVALID, "rubix_dust_av_bwd: null gas pointer");
+  const size_t need = rubix_dust_av_bwd_workspace_size(n_gas, n_segments, n_stars);
+  RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= need, RUBIX_E_WORKSPACE,
+                "rubix_dust_av_bwd: workspace of %zu bytes needed, %zu given", need,
+                workspace_bytes);
+  RUBIX_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, RUBIX_E_INVALID,
+                "rubix_dust_av_bwd: workspace must be 256-byte aligned");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_gas > 0)
+    RUBIX_CUDA_TRY(cudaMemsetAsync(grad_gas_ext, 0, sizeof(float) * (size_t)n_gas, st));
+  if (n_stars == 0) return RUBIX_OK;
+  const DustBwdLayout B = carve_dust_bwd(workspace, n_gas, n_segments, n_stars);
+  DustView v{};
+  {
+    const int rc = dust_setup(gas_coords, gas_stride, gas_pa, gas_ext, n_gas, n_segments,
+                              pa_limit, B.fwd, v, st);
+    if (rc != RUBIX_OK) return rc;
+  }
+  const long long star_blocks = (n_stars + 255) / 256;
+  dust_star_av_bwd_kernel<<<(unsigned)std::min<long long>(star_blocks, 1LL << 30), 256, 0,
+                            st>>>(v, star_coords, star_stride, star_pa, n_stars, grad_av,
+                                  grad_star_z, B.rk0, B.rv0, B.rw);
+  RUBIX_LAUNCH_CHECK("dust_star_av_bwd_kernel");
+  if (n_gas == 0) return RUBIX_OK;
+  // records by node, stable (the star order within a node), summed per node in order
+  const long long nr = 2 * n_stars;
+  const int w = radix_sort_pairs(B.rk0, B.rv0, B.rk1, B.rv1, nr, key_bits((unsigned)n_gas),
+                                 B.rhist, st);
+  const unsigned* rk = w ? B.rk1 : B.rk0;
+  const int* rv = w ? B.rv1 : B.rv0;
+  const long long tiles = (nr + kRunTile - 1) / kRunTile;
+  dust_run_partial_kernel<<<grid_for(tiles, 128), 128, 0, st>>>(rk, rv, B.rw, nr, B.partial);
+  RUBIX_CUDA_TRY(cudaMemsetAsync(B.gnode, 0, sizeof(double) * (size_t)n_gas, st));
+  dust_run_total_kernel<<<grid_for(tiles, 128), 128, 0, st>>>(rk, B.partial, nr,
+                                                              (unsigned)n_gas, B.gnode);
+  dust_suffix_kernel<<<grid_for((long long)n_segments * 32, 256), 256, 0, st>>>(
+      B.gnode, B.fwd.seg_off, n_segments, B.fwd.perm, grad_gas_ext);
+  RUBIX_LAUNCH_CHECK("dust A_V adjoint passes");
+  return RUBIX_OK;
+}
+
+extern "C" int rubix_dust_gas_extinction_bwd(const float* mass, const float* metals,
+                                             int64_t metals_stride, int32_t h_col,
+                                             int32_t o_col, int64_t n, const float* dgr_params,
+                                             int32_t broken, float scale, float spaxel_area,
+                                             const float* grad_ext, float* grad_mass,
+                                             float* grad_h, float* grad_o, void* stream) {
+  RUBIX_REQUIRE(n >= 0, RUBIX_E_INVALID, "rubix_dust_gas_extinction_bwd: n < 0");
+  RUBIX_REQUIRE(h_col >= 0 && o_col >= 0 && h_col < metals_stride && o_col < metals_stride,
+                RUBIX_E_INVALID, "rubix_dust_gas_extinction_bwd: H/O columns outside the rows");
+  RUBIX_REQUIRE(dgr_params != nullptr, RUBIX_E_INVALID,
+                "rubix_dust_gas_extinction_bwd: null dgr_params");
+  if (n == 0) return RUBIX_OK;
+  RUBIX_REQUIRE(mass && metals && grad_ext && grad_mass && grad_h && grad_o, RUBIX_E_INVALID,
+                "rubix_dust_gas_extinction_bwd: null pointer");
+  DgrParams p{dgr_params[0], dgr_params[1], dgr_params[2], dgr_params[3], dgr_params[4],
+              dgr_params[5], broken};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gas_extinction_bwd_kernel<<<grid_for(n, 256), 256, 0, st>>>(
+      mass, metals, metals_stride, h_col, o_col, n, p, scale, spaxel_area, grad_ext, grad_mass,
+      grad_h, grad_o);
+  RUBIX_LAUNCH_CHECK("gas_extinction_bwd_kernel");
   return RUBIX_OK;
 }
 

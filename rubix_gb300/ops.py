@@ -196,11 +196,11 @@ def cube_forward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, m
 
 def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, metallicity,
                   age, velocity, vel_component, perm, seg_offsets, n_segments, adj,
-                  dust_av=None, dust_exponent=None):
+                  dust_av=None, dust_exponent=None, av_grad=False):
     """Gradients (mass, metallicity, age, v_los) of <adj, cube> with cube the output of
-    ``cube_forward`` without LSF (with the same ``dust_av`` / ``dust_exponent``, A_V held
-    fixed); ``adj`` is [n_segments, >=L].  Four [n] tensors, zero for particles outside
-    the sorted set."""
+    ``cube_forward`` without LSF (with the same ``dust_av`` / ``dust_exponent``);
+    ``adj`` is [n_segments, >=L].  Four [n] tensors, zero for particles outside the
+    sorted set; with ``av_grad`` (dust only) a fifth, dL/dA_V of every particle."""
     ssp_flux = _contig("ssp_flux", ssp_flux, torch.float32)
     nz, na, nw = ssp_flux.shape
     ssp_metallicity = _contig("ssp_metallicity", ssp_metallicity, torch.float32)
@@ -222,7 +222,9 @@ def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, 
     if adj.dim() != 2 or adj.shape[0] != n_segments or adj.shape[1] < L or adj.stride(1) != 1:
         adj = adj.reshape(int(n_segments), -1).contiguous()
     dev = mass.device
-    grads = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(4)]
+    if av_grad and dust_av is None:
+        raise ValueError("av_grad needs dust_av and dust_exponent")
+    grads = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(5 if av_grad else 4)]
     nbytes = _lib.query("rubix_cube_bwd_workspace_size", n, int(n_segments), L, nz, na, nw)
     ws = workspace(nbytes, dev)
     if (dust_av is None) != (dust_exponent is None):
@@ -238,7 +240,8 @@ def cube_backward(ssp_flux, ssp_metallicity, ssp_age, ssp_wave_z, wave_t, mass, 
         dust_exponent = _contig("dust_exponent", dust_exponent, torch.float32).reshape(-1)
         if dust_av.numel() != n or dust_exponent.numel() != L:
             raise ValueError("dust_av must be [n] and dust_exponent [L]")
-        _lib.call("rubix_cube_bwd_dust", _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
+        _lib.call("rubix_cube_bwd_dust_av" if av_grad else "rubix_cube_bwd_dust",
+                  _ptr(ssp_flux), _ptr(ssp_metallicity), _ptr(ssp_age),
                   _ptr(ssp_wave_z), nz, na, nw, _ptr(wave_t), L, _ptr(mass), _ptr(metallicity),
                   _ptr(age), _ptr(velocity), vstride, int(vel_component), _ptr(dust_av),
                   _ptr(dust_exponent), _ptr(perm), _ptr(seg_offsets), int(n_segments), n,
@@ -585,6 +588,64 @@ def dust_av(gas_coords, gas_pa, gas_ext, star_coords, star_pa, n_segments: int,
                 k += 14 + 3 * _key_passes(int(n_segments) - 1)
         _count(k)
     return out
+
+
+def dust_av_backward(gas_coords, gas_pa, gas_ext, star_coords, star_pa, n_segments: int,
+                     pa_limit: int, grad_av):
+    """Adjoint of ``dust_av`` (``rubix_dust_av_bwd``): from dL/dA_V of every star, the
+    stars' dL/dz [n_stars] and the cells' dL/d ext [n_gas] (gas heights held fixed)."""
+    star_coords = _contig("star_coords", star_coords, torch.float32).reshape(-1, 3)
+    star_pa = _contig("star_pa", star_pa, torch.int32).reshape(-1)
+    gas_coords = _contig("gas_coords", gas_coords, torch.float32).reshape(-1, 3)
+    gas_pa = _contig("gas_pa", gas_pa, torch.int32).reshape(-1)
+    gas_ext = _contig("gas_ext", gas_ext, torch.float32).reshape(-1)
+    grad_av = _contig("grad_av", grad_av, torch.float32).reshape(-1)
+    ns, ng = star_coords.shape[0], gas_coords.shape[0]
+    if star_pa.numel() != ns or grad_av.numel() != ns or gas_pa.numel() != ng \
+            or gas_ext.numel() != ng:
+        raise ValueError("per-star / per-cell arrays must match the coordinates")
+    dev = star_coords.device
+    gz = torch.empty(ns, dtype=torch.float32, device=dev)
+    gext = torch.empty(ng, dtype=torch.float32, device=dev)
+    ws = workspace(_lib.query("rubix_dust_av_bwd_workspace_size", ng, int(n_segments), ns),
+                   dev)
+    _lib.call("rubix_dust_av_bwd", _ptr(gas_coords), 3, _ptr(gas_pa), _ptr(gas_ext), ng,
+              _ptr(star_coords), 3, _ptr(star_pa), ns, int(n_segments), int(pa_limit),
+              _ptr(grad_av), _ptr(gz), _ptr(gext), _ptr(ws), ws.numel(), _stream(dev))
+    if ns > 0:
+        k = 1
+        if ng > 0:
+            # the forward's setup passes, then the record sort and three reduction passes
+            k += 36 + 3 * _key_passes(int(pa_limit) - 1) + 3 + 3 * _key_passes(ng)
+            if pa_limit > n_segments:
+                k += 14 + 3 * _key_passes(int(n_segments) - 1)
+        _count(k)
+    return gz, gext
+
+
+def dust_gas_extinction_backward(mass, metals, dgr_params, broken: bool, scale: float,
+                                 spaxel_area: float, grad_ext, h_col: int = 0,
+                                 o_col: int = 4):
+    """Adjoint of ``dust_gas_extinction``: (dL/d mass [n], dL/d metals [n, columns], the
+    latter non-zero in the hydrogen and oxygen columns only)."""
+    mass = _contig("mass", mass, torch.float32).reshape(-1)
+    metals = _contig("metals", metals, torch.float32)
+    grad_ext = _contig("grad_ext", grad_ext, torch.float32).reshape(-1)
+    n = mass.numel()
+    rows = metals.reshape(n, -1) if n > 0 else metals.reshape(0, max(h_col, o_col) + 1)
+    prm = np.ascontiguousarray(np.asarray(dgr_params, dtype=np.float32).reshape(6))
+    dev = mass.device
+    gm = torch.empty(n, dtype=torch.float32, device=dev)
+    gh = torch.empty(n, dtype=torch.float32, device=dev)
+    go = torch.empty(n, dtype=torch.float32, device=dev)
+    _lib.call("rubix_dust_gas_extinction_bwd", _ptr(mass), _ptr(rows), rows.shape[1],
+              int(h_col), int(o_col), n, prm.ctypes.data, 1 if broken else 0, float(scale),
+              float(spaxel_area), _ptr(grad_ext), _ptr(gm), _ptr(gh), _ptr(go), _stream(dev))
+    _count(1 if n > 0 else 0)
+    gmet = torch.zeros_like(rows)
+    gmet[:, h_col] = gh
+    gmet[:, o_col] = go
+    return gm, gmet.view_as(metals)
 
 
 def dust_apply_rows_(rows: torch.Tensor, av, exponent) -> torch.Tensor:

@@ -184,3 +184,24 @@ def test_get_extinction_config_errors():
         get_extinction({"ssp": {}, "galaxy": {"dist_z": 0.1}})
     with pytest.raises(ValueError, match="Extinction model not found in dust configuration."):
         get_extinction({"ssp": {"dust": {}}, "galaxy": {"dist_z": 0.1}})
+
+
+def test_float64_mode_follows_the_float32_restatement():
+    """The float64 evaluation (used for differences) takes the same steps: A_V and the
+    per-cell extinction agree with the float32 restatement to float32 rounding."""
+    from rubix_gb300 import synth
+
+    rng = np.random.Generator(np.random.PCG64(11))
+    gz = rng.normal(0.0, 1.0, 400).astype(np.float32)
+    sz = rng.normal(0.0, 1.5, 600).astype(np.float32)
+    gpa = rng.integers(0, 9, 400).astype(np.int32)
+    spa = rng.integers(0, 9, 600).astype(np.int32)
+    gext = rng.uniform(0.0, 0.2, 400).astype(np.float32)
+    a32 = do.spaxel_av(gz, gpa, gext, sz, spa, 9)
+    a64 = do.spaxel_av(gz, gpa, gext, sz, spa, 9, dtype=np.float64)
+    assert a64.dtype == np.float64
+    assert np.max(np.abs(a64 - a32)) <= 1e-5 * np.max(np.abs(a32))
+    g = synth.make_gas(1000, seed=2)
+    e32 = do.gas_extinction(g.mass, g.metals, 0.1)
+    e64 = do.gas_extinction(g.mass, g.metals, 0.1, dtype=np.float64)
+    np.testing.assert_allclose(e64, e32, rtol=1e-5)
