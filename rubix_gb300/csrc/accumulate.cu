@@ -18,8 +18,8 @@
 //     pools of kPB * (nW + 2) entries.  One thread issues a 1-D TMA bulk copy of each
 //     particle's corner-table segment (its bracket range only) into the staging pool; it
 //     completes on an mbarrier while the block evaluates the previous batch.  The
-//     warps, split evenly over the batch's particles, then build per particle the row of
-//     entries (lambda'_k, slope_k, G_k, lambda'_{k+1}) of the mixed template
+//     threads, one group of 7 consecutive entries each, then build per particle the row
+//     of entries (lambda'_k, slope_k, G_k, lambda'_{k+1}) of the mixed template
 //     G = sum_c w_c F_c; the in-range flux sum T
 //     (rubix/spectra/ifu.py:241-245) comes from the gather (prefix sums).
 //   * Evaluation: each thread finds the exact bracket of its first wavelength (bucket
@@ -301,6 +301,121 @@ __device__ __forceinline__ void build_plan(const MainArgs& a, const ParticleRec*
   }
 }
 
+// Row builds from staged corners by groups: the entries of a batch's rows are cut into
+// groups of kBU consecutive entries of one particle, one group per thread.  A thread
+// mixes the template and shifts the wavelength of its kBU entries and of the right
+// neighbour itself (no shuffles, no per-warp row parameters), so an interior entry costs
+// two shared loads, the four-corner mix, one multiply, the slope and one store.
+// Consecutive threads are kBU entries apart; with kBU = 7 (112 bytes) the 16-byte loads
+// and stores of a quarter-warp fall in distinct banks.  Every entry is computed with the
+// arithmetic of build_step, so the rows equal build_plan's bit for bit.  Odd kBU keeps a
+// quarter-warp's entries in distinct banks; R = 6 and R = 11 take 5-entry groups, which
+// keep those kernels free of spills.  The dust kernels keep build_plan: next to the transmission
+// state, the group build spills there at any group length.
+template <int R>
+constexpr int build_group_len() {
+  return (R > 10 || R < 8) ? 5 : 7;
+}
+
+struct BuildPart {  // one particle of a planned batch, prepared once in shared memory
+  float w00, w10, w01, w11;
+  float alpha;
+  int ks, klo, khi;
+  int n_e, off, g0, has_cell;
+};
+
+// One thread: the build parameters of a planned batch and its total group count.
+// kstart >= -1 and kend >= kstart give khi >= klo, so the clamped corner index of every
+// entry lies in the particle's staged segment [klo, khi].
+template <int kBU>
+__device__ __forceinline__ void prep_parts(const ParticleRec* recs, const BatchPlan& bp, int nW,
+                                           BuildPart* out, int* gtot) {
+  int g = 0;
+  for (int p = 0; p < bp.cnt; ++p) {
+    const ParticleRec r = recs[p];
+    BuildPart q;
+    const float tz = r.a.w, ta = __int_as_float(r.b.w);
+    const int ke = r.b.z & ~kGenericFlag;
+    q.alpha = r.a.y;
+    q.w00 = (1.f - tz) * (1.f - ta);
+    q.w10 = tz * (1.f - ta);
+    q.w01 = (1.f - tz) * ta;
+    q.w11 = tz * ta;
+    q.ks = r.b.y;
+    q.klo = max(q.ks, 0);
+    q.khi = min(ke + 1, nW - 1);
+    q.n_e = ke - q.ks + 1;
+    q.has_cell = r.b.x >= 0;
+    q.off = p == 0 ? 0 : (p == 1 ? bp.off[1] : bp.off[2]);
+    q.g0 = g;
+    g += (q.n_e + kBU - 1) / kBU;
+    out[p] = q;
+  }
+  *gtot = g;
+}
+
+// G = sum_c w_c F_c of one staged entry (0 for particles outside the SSP grid: their
+// staging slot holds no copy, and the select discards whatever it holds).
+__device__ __forceinline__ float mix_corners(const BuildPart& q, const float4 c) {
+  float G = q.w00 * c.x;
+  G = fmaf(q.w10, c.y, G);
+  G = fmaf(q.w01, c.z, G);
+  G = fmaf(q.w11, c.w, G);
+  return q.has_cell ? G : 0.f;
+}
+
+template <int kBU>
+__device__ __forceinline__ void build_groups(const MainArgs& a,
+                                             const BuildPart* __restrict__ parts, int cnt,
+                                             int gtot, const float* __restrict__ s_wz,
+                                             const float4* __restrict__ stage,
+                                             float4* __restrict__ rows, int tid) {
+  const int nW = a.n_wave;
+  for (int g = tid; g < gtot; g += kAccThreads) {
+    const int p = (cnt > 2 && g >= parts[2].g0) ? 2 : ((cnt > 1 && g >= parts[1].g0) ? 1 : 0);
+    const BuildPart q = parts[p];
+    const int e0 = (g - q.g0) * kBU;
+    const int k0 = q.ks + e0;
+    const float4* st = stage + q.off - q.klo;  // st[k]: staged corners, k in [klo, khi]
+    float4* row = rows + q.off;
+    if (k0 >= 0 && k0 + kBU <= q.khi && e0 + kBU <= q.n_e) {
+      // interior group: every entry and its neighbour are SSP wavelengths of the range
+      float Gv[kBU + 1], Lv[kBU + 1];
+#pragma unroll
+      for (int j = 0; j <= kBU; ++j) {
+        Gv[j] = mix_corners(q, st[k0 + j]);
+        Lv[j] = __fmul_rn(s_wz[k0 + j], q.alpha);
+      }
+#pragma unroll
+      for (int j = 0; j < kBU; ++j) {
+        const float dl = Lv[j + 1] - Lv[j];
+        const float slope = dl > 0.f ? __fdividef(Gv[j + 1] - Gv[j], dl) : 0.f;
+        row[e0 + j] = make_float4(Lv[j], slope, Gv[j], Lv[j + 1]);
+      }
+    } else {
+      // ends of the row: clamped corners and the sentinels of build_step
+      for (int j = 0; j < kBU; ++j) {
+        const int e = e0 + j;
+        if (e >= q.n_e) break;
+        const int k = q.ks + e;
+        const float G = mix_corners(q, st[min(max(k, q.klo), q.khi)]);
+        const float Gn = mix_corners(q, st[min(max(k + 1, q.klo), q.khi)]);
+        const float lp = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(s_wz[k], q.alpha));
+        const int k1 = k + 1;
+        const float lpn =
+            (k1 < 0) ? -kFltMax : (k1 >= nW ? kFltMax : __fmul_rn(s_wz[k1], q.alpha));
+        float slope = 0.f;
+        if (k >= 0 && k + 1 < nW) {
+          const float dl = lpn - lp;
+          slope = dl > 0.f ? __fdividef(Gn - G, dl) : 0.f;
+        }
+        const float lpw = (k + 1 >= nW) ? kFltMax : lpn;
+        row[e] = make_float4(lp, slope, G, lpw);
+      }
+    }
+  }
+}
+
 // Sums 4 values over the 32 lanes with 6 shuffles; lane 0 ends with the total of v0,
 // lane 8 with v1, lane 16 with v2, lane 24 with v3.
 __device__ __forceinline__ float warp_reduce4(float v0, float v1, float v2, float v3, int lane) {
@@ -494,6 +609,8 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   float* s_spec = reinterpret_cast<float*>(s_rows);  // LSF epilogue reuses the rows
   __shared__ uint64_t s_bar;
   __shared__ int s_item, s_last, s_fail;
+  __shared__ BuildPart s_bp[2][kPBMax];  // staged path: build parameters per batch buffer
+  __shared__ int s_gtot[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if constexpr (kStaged)
@@ -510,6 +627,8 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   const int t0 = tid * R;
   const int P = a.pool;
   constexpr bool staged = kStaged;
+  constexpr int kBU = build_group_len<R>();
+  constexpr bool kGroups = kStaged && !kDust;  // rows built by groups of kBU entries
   float lam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -544,6 +663,11 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
     __syncthreads();
     BatchPlan bp = plan_batch(s_rec, np, P);
     if (staged && np > 0 && tid == 0) issue_plan(a, s_rec, bp, s_stage, &s_bar);
+    if constexpr (kGroups) {
+      // warp 1 prepares the build parameters while warp 0 issues the copies
+      if (tid == 32) prep_parts<kBU>(s_rec, bp, a.n_wave, s_bp[step & 1], &s_gtot[step & 1]);
+      __syncthreads();
+    }
 
     // Batch at p0: wait for its staged corners, build its rows, stage the next batch,
     // evaluate, reduce T'.
@@ -555,7 +679,10 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
         if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
         phase ^= 1u;
       }
-      build_plan<kStaged>(a, recs, bp, wzp, s_stage, s_rows, lane, warp);
+      if constexpr (kGroups)
+        build_groups<kBU>(a, s_bp[buf], cnt, s_gtot[buf], wzp, s_stage, s_rows, tid);
+      else
+        build_plan<kStaged>(a, recs, bp, wzp, s_stage, s_rows, lane, warp);
       __syncthreads();  // rows ready; staging consumed
       if (s_fail) {
         if (tid == 0) {
@@ -567,6 +694,11 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
       const int p1 = p0 + cnt;
       const BatchPlan bn = plan_batch(s_rec + p1, np - p1, P);
       if (staged && p1 < np && tid == 0) issue_plan(a, s_rec + p1, bn, s_stage, &s_bar);
+      // the other buffer: last read by the previous batch's build, before the barrier
+      // above; read by the next build after the T' reduction barrier below
+      if constexpr (kGroups)
+        if (tid == 32)
+          prep_parts<kBU>(s_rec + p1, bn, a.n_wave, s_bp[buf ^ 1], &s_gtot[buf ^ 1]);
 
       float I[kPBMax][R];
       float tp[kPBMax];
