@@ -322,6 +322,7 @@ struct BuildPart {  // one particle of a planned batch, prepared once in shared 
   float alpha;
   int ks, klo, khi;
   int n_e, off, g0, has_cell;
+  int plain;  // kstart >= 0 and kend + 1 <= nW - 1: the row touches neither grid end
 };
 
 // One thread: the build parameters of a planned batch and its total group count.
@@ -346,6 +347,7 @@ __device__ __forceinline__ void prep_parts(const ParticleRec* recs, const BatchP
     q.khi = min(ke + 1, nW - 1);
     q.n_e = ke - q.ks + 1;
     q.has_cell = r.b.x >= 0;
+    q.plain = q.ks >= 0 && ke + 1 <= nW - 1;
     q.off = p == 0 ? 0 : (p == 1 ? bp.off[1] : bp.off[2]);
     q.g0 = g;
     g += (q.n_e + kBU - 1) / kBU;
@@ -378,7 +380,25 @@ __device__ __forceinline__ void build_groups(const MainArgs& a,
     const int k0 = q.ks + e0;
     const float4* st = stage + q.off - q.klo;  // st[k]: staged corners, k in [klo, khi]
     float4* row = rows + q.off;
-    if (k0 >= 0 && k0 + kBU <= q.khi && e0 + kBU <= q.n_e) {
+    if (q.plain) {
+      // every stored entry k <= kend and its neighbour k + 1 <= kend + 1 = khi are in the
+      // staged segment.  The entries of a last, partial group past the row's end are
+      // computed and not stored; their loads stay in shared memory (at most kBU - 2
+      // float4 past the staging pool, which the row pool follows, and kBU - 1 floats past
+      // the SSP wavelengths, which the bucket table follows).
+      float Gv[kBU + 1], Lv[kBU + 1];
+#pragma unroll
+      for (int j = 0; j <= kBU; ++j) {
+        Gv[j] = mix_corners(q, st[k0 + j]);
+        Lv[j] = __fmul_rn(s_wz[k0 + j], q.alpha);
+      }
+#pragma unroll
+      for (int j = 0; j < kBU; ++j) {
+        const float dl = Lv[j + 1] - Lv[j];
+        const float slope = dl > 0.f ? __fdividef(Gv[j + 1] - Gv[j], dl) : 0.f;
+        if (e0 + j < q.n_e) row[e0 + j] = make_float4(Lv[j], slope, Gv[j], Lv[j + 1]);
+      }
+    } else if (k0 >= 0 && k0 + kBU <= q.khi && e0 + kBU <= q.n_e) {
       // interior group: every entry and its neighbour are SSP wavelengths of the range
       float Gv[kBU + 1], Lv[kBU + 1];
 #pragma unroll
