@@ -317,13 +317,15 @@ constexpr int build_group_len() {
   return (R > 10 || R < 8) ? 5 : 7;
 }
 
-struct BuildPart {  // one particle of a planned batch, prepared once in shared memory
-  float w00, w10, w01, w11;
-  float alpha;
-  int ks, klo, khi;
-  int n_e, off, g0, has_cell;
-  int plain;  // kstart >= 0 and kend + 1 <= nW - 1: the row touches neither grid end
+// One particle of a planned batch, prepared once in shared memory as three 16-byte
+// vectors (three vector loads per group instead of a dozen scalar ones).
+struct __align__(16) BuildPart {
+  float4 w;  // bilinear weights w00, w10, w01, w11
+  int4 a;    // first group g0, kstart, staging offset - klo, row offset
+  int4 b;    // n_e, flags (kPartCell | kPartPlain), khi, alpha (bits)
 };
+constexpr int kPartCell = 1;   // inside the SSP grid (else G = 0)
+constexpr int kPartPlain = 2;  // kstart >= 0 and kend + 1 <= nW - 1: no grid end in the row
 
 // One thread: the build parameters of a planned batch and its total group count.
 // kstart >= -1 and kend >= kstart give khi >= klo, so the clamped corner index of every
@@ -337,20 +339,16 @@ __device__ __forceinline__ void prep_parts(const ParticleRec* recs, const BatchP
     BuildPart q;
     const float tz = r.a.w, ta = __int_as_float(r.b.w);
     const int ke = r.b.z & ~kGenericFlag;
-    q.alpha = r.a.y;
-    q.w00 = (1.f - tz) * (1.f - ta);
-    q.w10 = tz * (1.f - ta);
-    q.w01 = (1.f - tz) * ta;
-    q.w11 = tz * ta;
-    q.ks = r.b.y;
-    q.klo = max(q.ks, 0);
-    q.khi = min(ke + 1, nW - 1);
-    q.n_e = ke - q.ks + 1;
-    q.has_cell = r.b.x >= 0;
-    q.plain = q.ks >= 0 && ke + 1 <= nW - 1;
-    q.off = p == 0 ? 0 : (p == 1 ? bp.off[1] : bp.off[2]);
-    q.g0 = g;
-    g += (q.n_e + kBU - 1) / kBU;
+    const int ks = r.b.y;
+    const int klo = max(ks, 0);
+    const int n_e = ke - ks + 1;
+    const int off = p == 0 ? 0 : (p == 1 ? bp.off[1] : bp.off[2]);
+    q.w = make_float4((1.f - tz) * (1.f - ta), tz * (1.f - ta), (1.f - tz) * ta, tz * ta);
+    q.a = make_int4(g, ks, off - klo, off);
+    q.b = make_int4(n_e,
+                    (r.b.x >= 0 ? kPartCell : 0) | ((ks >= 0 && ke + 1 <= nW - 1) ? kPartPlain : 0),
+                    min(ke + 1, nW - 1), __float_as_int(r.a.y));
+    g += (n_e + kBU - 1) / kBU;
     out[p] = q;
   }
   *gtot = g;
@@ -358,12 +356,12 @@ __device__ __forceinline__ void prep_parts(const ParticleRec* recs, const BatchP
 
 // G = sum_c w_c F_c of one staged entry (0 for particles outside the SSP grid: their
 // staging slot holds no copy, and the select discards whatever it holds).
-__device__ __forceinline__ float mix_corners(const BuildPart& q, const float4 c) {
-  float G = q.w00 * c.x;
-  G = fmaf(q.w10, c.y, G);
-  G = fmaf(q.w01, c.z, G);
-  G = fmaf(q.w11, c.w, G);
-  return q.has_cell ? G : 0.f;
+__device__ __forceinline__ float mix_corners(const float4 w, bool has_cell, const float4 c) {
+  float G = w.x * c.x;
+  G = fmaf(w.y, c.y, G);
+  G = fmaf(w.z, c.z, G);
+  G = fmaf(w.w, c.w, G);
+  return has_cell ? G : 0.f;
 }
 
 template <int kBU>
@@ -374,56 +372,50 @@ __device__ __forceinline__ void build_groups(const MainArgs& a,
                                              float4* __restrict__ rows, int tid) {
   const int nW = a.n_wave;
   for (int g = tid; g < gtot; g += kAccThreads) {
-    const int p = (cnt > 2 && g >= parts[2].g0) ? 2 : ((cnt > 1 && g >= parts[1].g0) ? 1 : 0);
-    const BuildPart q = parts[p];
-    const int e0 = (g - q.g0) * kBU;
-    const int k0 = q.ks + e0;
-    const float4* st = stage + q.off - q.klo;  // st[k]: staged corners, k in [klo, khi]
-    float4* row = rows + q.off;
-    if (q.plain) {
-      // every stored entry k <= kend and its neighbour k + 1 <= kend + 1 = khi are in the
-      // staged segment.  The entries of a last, partial group past the row's end are
-      // computed and not stored; their loads stay in shared memory (at most kBU - 2
-      // float4 past the staging pool, which the row pool follows, and kBU - 1 floats past
-      // the SSP wavelengths, which the bucket table follows).
+    const int p = (cnt > 2 && g >= parts[2].a.x) ? 2 : ((cnt > 1 && g >= parts[1].a.x) ? 1 : 0);
+    const int4 qa = parts[p].a;
+    const int4 qb = parts[p].b;
+    const float4 w = parts[p].w;
+    const bool has_cell = (qb.y & kPartCell) != 0;
+    const float alpha = __int_as_float(qb.w);
+    const int ks = qa.y, n_e = qb.x, khi = qb.z;
+    const int e0 = (g - qa.x) * kBU;
+    const int k0 = ks + e0;
+    const float4* st = stage + qa.z;  // st[k]: staged corners, k in [klo, khi]
+    float4* row = rows + qa.w;
+    if ((qb.y & kPartPlain) || (k0 >= 0 && k0 + kBU <= khi && e0 + kBU <= n_e)) {
+      // A row that touches neither grid end: every stored entry k <= kend and its
+      // neighbour k + 1 <= kend + 1 = khi are in the staged segment.  The entries of a
+      // last, partial group past the row's end are computed and not stored; their loads
+      // stay in shared memory (at most kBU - 2 float4 past the staging pool, which the
+      // row pool follows, and kBU - 1 floats past the SSP wavelengths, which the bucket
+      // table follows).  Otherwise an interior group: every entry and its neighbour are
+      // SSP wavelengths of the staged range, and every entry is stored.
       float Gv[kBU + 1], Lv[kBU + 1];
 #pragma unroll
       for (int j = 0; j <= kBU; ++j) {
-        Gv[j] = mix_corners(q, st[k0 + j]);
-        Lv[j] = __fmul_rn(s_wz[k0 + j], q.alpha);
+        Gv[j] = mix_corners(w, has_cell, st[k0 + j]);
+        Lv[j] = __fmul_rn(s_wz[k0 + j], alpha);
       }
 #pragma unroll
       for (int j = 0; j < kBU; ++j) {
         const float dl = Lv[j + 1] - Lv[j];
         const float slope = dl > 0.f ? __fdividef(Gv[j + 1] - Gv[j], dl) : 0.f;
-        if (e0 + j < q.n_e) row[e0 + j] = make_float4(Lv[j], slope, Gv[j], Lv[j + 1]);
-      }
-    } else if (k0 >= 0 && k0 + kBU <= q.khi && e0 + kBU <= q.n_e) {
-      // interior group: every entry and its neighbour are SSP wavelengths of the range
-      float Gv[kBU + 1], Lv[kBU + 1];
-#pragma unroll
-      for (int j = 0; j <= kBU; ++j) {
-        Gv[j] = mix_corners(q, st[k0 + j]);
-        Lv[j] = __fmul_rn(s_wz[k0 + j], q.alpha);
-      }
-#pragma unroll
-      for (int j = 0; j < kBU; ++j) {
-        const float dl = Lv[j + 1] - Lv[j];
-        const float slope = dl > 0.f ? __fdividef(Gv[j + 1] - Gv[j], dl) : 0.f;
-        row[e0 + j] = make_float4(Lv[j], slope, Gv[j], Lv[j + 1]);
+        if (e0 + j < n_e) row[e0 + j] = make_float4(Lv[j], slope, Gv[j], Lv[j + 1]);
       }
     } else {
       // ends of the row: clamped corners and the sentinels of build_step
+      const int klo = max(ks, 0);
       for (int j = 0; j < kBU; ++j) {
         const int e = e0 + j;
-        if (e >= q.n_e) break;
-        const int k = q.ks + e;
-        const float G = mix_corners(q, st[min(max(k, q.klo), q.khi)]);
-        const float Gn = mix_corners(q, st[min(max(k + 1, q.klo), q.khi)]);
-        const float lp = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(s_wz[k], q.alpha));
+        if (e >= n_e) break;
+        const int k = ks + e;
+        const float G = mix_corners(w, has_cell, st[min(max(k, klo), khi)]);
+        const float Gn = mix_corners(w, has_cell, st[min(max(k + 1, klo), khi)]);
+        const float lp = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(s_wz[k], alpha));
         const int k1 = k + 1;
         const float lpn =
-            (k1 < 0) ? -kFltMax : (k1 >= nW ? kFltMax : __fmul_rn(s_wz[k1], q.alpha));
+            (k1 < 0) ? -kFltMax : (k1 >= nW ? kFltMax : __fmul_rn(s_wz[k1], alpha));
         float slope = 0.f;
         if (k >= 0 && k + 1 < nW) {
           const float dl = lpn - lp;
