@@ -444,6 +444,15 @@ RUBIX_API int rubix_segment_sum_rows(const float* rows, int64_t row_stride, int3
 RUBIX_API int rubix_psf_fwd(const float* in, float* out, int32_t ny, int32_t nx, int32_t n_wave_t,
                   int64_t spaxel_stride_in, int64_t spaxel_stride_out, const float* ty,
                   int32_t m_y, const float* tx, int32_t m_x, void* stream);
+/*
+ * With m_y = m_x <= 17, a 16-byte aligned `in` and spaxel_stride_in a multiple of 4
+ * floats (e.g. n_wave_t rounded up to a multiple of 4), the input rows are staged by
+ * tiled TMA copies; a staged-row wait that runs out (about 1 s) makes the kernel set a
+ * device error word and return.  rubix_psf_status reads that word (synchronises
+ * `stream`): *device_error = 1 and RUBIX_E_DEVICE if it was set since the last read,
+ * which clears it; 0 and RUBIX_OK otherwise.
+ */
+RUBIX_API int rubix_psf_status(int* device_error, void* stream);
 
 /* ------------------------------------------------------------------------- */
 /* (d) LSF: 1-D convolution along wavelength                                 */

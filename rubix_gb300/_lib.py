@@ -83,6 +83,7 @@ SIGNATURES = {
     "rubix_psf_fwd": (
         _c.c_int, [_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _vp, _i32, _vp]
     ),
+    "rubix_psf_status": (_c.c_int, [_c.POINTER(_c.c_int), _vp]),
     "rubix_lsf_fwd": (_c.c_int, [_vp, _vp, _i64, _i32, _i64, _i64, _vp, _i32, _i32, _vp]),
     "rubix_cube_bwd_workspace_size": (_sz, [_i64, _i32, _i32, _i32, _i32, _i32]),
     "rubix_cube_bwd": (

@@ -142,10 +142,25 @@ class IFURenderer:
         return ops.dust_av(gc, gidx, gext, _dev(star_coords, self.device), star_idx, nseg,
                            max(nb * nb, nseg))
 
+    def cube_buffer(self) -> torch.Tensor:
+        """An uninitialised [sbin*sbin, L] float32 buffer for ``accumulate(out=...)``.  With a
+        PSF its spaxel stride is L rounded up to a multiple of 4 floats, so the PSF stages
+        the cube's rows with tiled TMA copies (16-byte row strides); the view is [.., L]
+        and the padding is never read.  ``.contiguous()`` gives the dense layout."""
+        n, L = self.sbin * self.sbin, self.n_wave_t
+        if self.psf_taps is None:
+            return torch.empty((n, L), dtype=torch.float32, device=self.device)
+        buf = torch.empty((n, (L + 3) // 4 * 4), dtype=torch.float32, device=self.device)
+        return buf[:, :L]
+
     def accumulate(self, mass, metallicity, age, velocity, perm, seg_offsets, out=None,
                    with_lsf=False, dust_av=None):
         """Fused lookup/mass/Doppler/resample/sum; ``with_lsf`` adds the LSF epilogue and
-        ``dust_av`` (A_V per particle) the dust transmission of each spectrum."""
+        ``dust_av`` (A_V per particle) the dust transmission of each spectrum.  Without
+        ``out`` the cube goes to ``cube_buffer()``: with a PSF, a [sbin, sbin, L] view
+        whose spaxel stride is L rounded up to a multiple of 4."""
+        if out is None:
+            out = self.cube_buffer()
         cube = ops.cube_forward(self.ssp_flux, self.ssp_metallicity, self.ssp_age, self.ssp_wave_z,
                                 self.wave_t, _dev(mass, self.device), _dev(metallicity, self.device),
                                 _dev(age, self.device), _dev(velocity, self.device),
@@ -257,8 +272,7 @@ class HostStream:
         fuse = r.lsf_taps is not None
         if slot["cube"] is None:
             L = r.n_wave_t
-            slot["cube"] = torch.empty((r.sbin * r.sbin, L), dtype=torch.float32,
-                                       device=r.device)
+            slot["cube"] = r.cube_buffer()
             slot["final"] = torch.empty((r.sbin, r.sbin, L), dtype=torch.float32,
                                         device=r.device)
         cube = r.accumulate(m, z, a, v, perm, offs, out=slot["cube"], with_lsf=fuse)

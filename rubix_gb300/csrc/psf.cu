@@ -10,7 +10,13 @@
 // memory with its x halo, convolved along x into a ring of the last m_y rows, and
 // the ring gives the y-convolved output row.  Every input element is read from
 // global memory once per strip (plus the x halo) and every output written once.
+// When the input's spaxel stride is a multiple of 16 bytes, one thread stages each row
+// with a single tiled TMA copy (psf_tma_kernel); otherwise every thread issues 4-byte
+// cp.async copies of its share of the row.
 #include "common.cuh"
+#include "tma.cuh"
+
+#include <cuda.h>  // CUtensorMap and its enums; cuTensorMapEncodeTiled comes through the runtime
 
 namespace rubix {
 namespace {
@@ -346,6 +352,174 @@ __global__ void __launch_bounds__(kPsfThreads, 2) psf_reg2_kernel(PsfArgs a) {
   cp_async_wait<0>();
 }
 
+// Device error word of the TMA-staged PSF: set when a bounded wait for a staged row
+// runs out (the block then waits for its copies in flight and returns without writing
+// the rest of its strip).  Sticky until rubix_psf_status reads it.
+__device__ int g_psf_error;
+
+// The strip of psf_reg2_kernel with its input rows staged by TMA: thread 0 loads input
+// row r (W spaxel columns from x0 - (M-1) + ox, kTileL wavelengths from l0, zero outside
+// the cube) with one tiled copy of the 3-D tensor map (wavelength, x, y) into ring slot
+// r % S, completing on that slot's mbarrier, S - 1 rows ahead.  The copies replace the
+// per-thread 4-byte copies, their address arithmetic and validity masks.  The
+// wavelength coordinate l0 is a multiple of 32 floats (128 bytes), as a tiled copy
+// needs; x and y may start outside the cube, where the copy fills zeros.  Same products
+// and summation order as psf_reg2_kernel: bit-identical.
+// Ring depth of the TMA-staged kernel: as many staged rows as fit in 48 KB of static
+// shared memory next to the slots' mbarriers, at most 8.
+__host__ __device__ constexpr int psf_tma_stages(int M) {
+  return (48 * 1024 - 256) / ((kPsfTileX + M - 1) * kPsfTileL * 4) >= 8
+             ? 8
+             : (48 * 1024 - 256) / ((kPsfTileX + M - 1) * kPsfTileL * 4);
+}
+
+template <int M>
+__global__ void __launch_bounds__(kPsfThreads, 2)
+    psf_tma_kernel(const __grid_constant__ CUtensorMap map, PsfArgs a) {
+  constexpr int W = kPsfTileX + M - 1;  // staged row width
+  constexpr int kS = psf_tma_stages(M);
+  static_assert(kS >= 3, "PSF ring needs at least 3 rows");
+  constexpr int NA = (kPsfXB + M - 1) / 2;  // aligned input pairs per thread and row
+  constexpr uint32_t kRowBytes = W * kPsfTileL * sizeof(float);
+  static_assert(kPsfXB == 4 && (M & 1), "two output pairs, odd tap count");
+  static_assert((W * kPsfTileL * sizeof(float)) % 128 == 0, "ring slots stay 128-byte aligned");
+  __shared__ __align__(128) float s_in[kS][W * kPsfTileL];
+  __shared__ uint64_t s_bar[kS];
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float* __restrict__ out = a.out;
+  const int ny = a.ny, nx = a.nx, nl = a.nl, oy = a.oy;
+  const long long sout = a.sout;
+  const int x0 = blockIdx.x * kPsfTileX;
+  const int l0 = blockIdx.y * kPsfTileL;
+  const int l = l0 + lane;
+  const int xsrc0 = x0 - (M - 1) + a.ox;
+  const int xb = warp * kPsfXB;
+  const int total = ny + oy;  // input rows 0 .. ny-1+oy (rows >= ny are zero)
+  if (tid == 0) {
+    for (int i = 0; i < kS; ++i) mbar_init(&s_bar[i], 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    fence_proxy_async_smem();
+    for (int r = 0; r < kS - 1 && r < total; ++r) {
+      mbar_arrive_expect_tx(&s_bar[r], kRowBytes);
+      tensor_copy_3d_g2s(s_in[r], &map, l0, xsrc0, r, &s_bar[r]);
+    }
+  }
+  float2 win[M][2];  // x-convolved rows r-M+1 .. r of this thread's two output pairs
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    win[i][0] = make_float2(0.f, 0.f);
+    win[i][1] = win[i][0];
+  }
+  for (int r0 = 0; r0 < total; r0 += M) {
+#pragma unroll
+    for (int jj = 0; jj < M; ++jj) {
+      const int r = r0 + jj;
+      if (r >= total) break;
+      const int slot = r % kS;
+      if (!mbar_wait_bounded(&s_bar[slot], (uint32_t)(r / kS) & 1u)) s_fail = 1;
+      __syncthreads();  // row r landed for every thread; row r - 1 is consumed
+      if (s_fail) {
+        if (tid == 0) {
+          atomicExch(&g_psf_error, 1);
+          for (int q = r; q < r + kS - 1 && q < total; ++q)  // rows still in flight
+            mbar_wait_bounded(&s_bar[q % kS], (uint32_t)(q / kS) & 1u);
+        }
+        return;
+      }
+      if (tid == 0) {  // row r + S - 1 into the slot row r - 1 left
+        const int rn = r + kS - 1;
+        if (rn < total) {
+          fence_proxy_async_smem();
+          mbar_arrive_expect_tx(&s_bar[rn % kS], kRowBytes);
+          tensor_copy_3d_g2s(s_in[rn % kS], &map, l0, xsrc0, rn, &s_bar[rn % kS]);
+        }
+      }
+      const float* row = s_in[slot];
+      float2 A[NA], B[NA - 1];
+#pragma unroll
+      for (int m = 0; m < NA; ++m) {
+        A[m].x = row[(xb + 2 * m) * kPsfTileL + lane];
+        A[m].y = row[(xb + 2 * m + 1) * kPsfTileL + lane];
+      }
+#pragma unroll
+      for (int m = 0; m < NA - 1; ++m) B[m] = make_float2(A[m].y, A[m + 1].x);
+      float2 h0 = make_float2(0.f, 0.f), h1 = h0;
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        const float2 t = make_float2(a.tx[i], a.tx[i]);
+        const int k0 = M - 1 - i, k1 = M + 1 - i;  // first input of outputs 0-1 and 2-3
+        h0 = __ffma2_rn(t, (k0 & 1) ? B[k0 >> 1] : A[k0 >> 1], h0);
+        h1 = __ffma2_rn(t, (k1 & 1) ? B[k1 >> 1] : A[k1 >> 1], h1);
+      }
+      win[jj][0] = h0;
+      win[jj][1] = h1;
+      const int y = r - oy;
+      if (y >= 0 && l < nl) {
+        float2 o0 = make_float2(0.f, 0.f), o1 = o0;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const float2 t = make_float2(a.ty[i], a.ty[i]);
+          o0 = __ffma2_rn(t, win[(jj - i + M) % M][0], o0);
+          o1 = __ffma2_rn(t, win[(jj - i + M) % M][1], o1);
+        }
+        const int x = x0 + xb;
+        float* o = out + ((long long)y * nx + x) * sout + l;
+        if (x < nx) o[0] = o0.x;
+        if (x + 1 < nx) o[sout] = o0.y;
+        if (x + 2 < nx) o[2 * sout] = o1.x;
+        if (x + 3 < nx) o[3 * sout] = o1.y;
+      }
+    }
+  }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry points (null if unavailable).
+EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                                           cudaEnableDefault, &q);
+    return (e == cudaSuccess && q == cudaDriverEntryPointSuccess)
+               ? reinterpret_cast<EncodeTiledFn>(f)
+               : nullptr;
+  }();
+  return fn;
+}
+
+// The TMA-staged kernel when the input allows tiled copies (16-byte aligned base, spaxel
+// stride a multiple of 4 floats); false (nothing launched) otherwise.
+template <int M>
+bool launch_psf_tma(const PsfArgs& a, cudaStream_t st) {
+  if (a.sin % 4 != 0 || (reinterpret_cast<uintptr_t>(a.in) & 15) != 0) return false;
+  const EncodeTiledFn enc = encode_tiled();
+  if (enc == nullptr) return false;
+  constexpr int W = kPsfTileX + M - 1;
+  CUtensorMap map;
+  const cuuint64_t dims[3] = {(cuuint64_t)a.nl, (cuuint64_t)a.nx, (cuuint64_t)a.ny};
+  const cuuint64_t strides[2] = {(cuuint64_t)a.sin * sizeof(float),
+                                 (cuuint64_t)a.nx * (cuuint64_t)a.sin * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)kPsfTileL, (cuuint32_t)W, 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(a.in), dims, strides, box,
+          elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  dim3 grid(div_up(a.nx, kPsfTileX), div_up(a.nl, kPsfTileL));
+  psf_tma_kernel<M><<<grid, kPsfThreads, 0, st>>>(map, a);
+  return true;
+}
+
 // Ragged batch: galaxy g owns blocks [block_off[g], block_off[g+1]) (x strips fastest),
 // its square S_g x S_g cube starts at spaxel seg_base[g], and its taps are
 // taps[g][0][:] (y) and taps[g][1][:] (x), zero-padded and centred to M.
@@ -383,8 +557,12 @@ template <int M>
 int launch_psf_reg(const PsfArgs& a, cudaStream_t st) {
   dim3 grid(div_up(a.nx, kPsfTileX), div_up(a.nl, kPsfTileL));
   // host taps: the packed-FMA kernel with the taps as parameters (up to 17 taps, where
-  // its window stays in registers)
+  // its window stays in registers), its rows staged by TMA where the stride allows
   if (a.ty_dev == nullptr && M <= 17) {
+    if (launch_psf_tma<(M <= 17 ? M : 17)>(a, st)) {
+      RUBIX_LAUNCH_CHECK("psf_tma_kernel");
+      return RUBIX_OK;
+    }
     psf_reg2_kernel<(M <= 17 ? M : 17)><<<grid, kPsfThreads, 0, st>>>(a);
     RUBIX_LAUNCH_CHECK("psf_reg2_kernel");
     return RUBIX_OK;
@@ -482,6 +660,22 @@ extern "C" int rubix_psf_fwd_dtaps(const float* in, float* out, int32_t ny, int3
                                    const float* tx, int32_t m_x, void* stream) {
   return psf_fwd_impl(in, out, ny, nx, n_wave_t, spaxel_stride_in, spaxel_stride_out, ty, m_y,
                       tx, m_x, true, stream);
+}
+
+extern "C" int rubix_psf_status(int* device_error, void* stream) {
+  RUBIX_REQUIRE(device_error != nullptr, RUBIX_E_INVALID, "rubix_psf_status: null pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int v = 0;
+  RUBIX_CUDA_TRY(cudaMemcpyFromSymbolAsync(&v, g_psf_error, sizeof(int), 0,
+                                           cudaMemcpyDeviceToHost, st));
+  RUBIX_CUDA_TRY(cudaStreamSynchronize(st));
+  *device_error = v;
+  if (v == 0) return RUBIX_OK;
+  const int zero = 0;
+  RUBIX_CUDA_TRY(cudaMemcpyToSymbolAsync(g_psf_error, &zero, sizeof(int), 0,
+                                         cudaMemcpyHostToDevice, st));
+  RUBIX_CUDA_TRY(cudaStreamSynchronize(st));
+  return set_error(RUBIX_E_DEVICE, "psf kernel: a TMA wait timed out");
 }
 
 extern "C" int rubix_ragged_psf_fwd(const float* in, float* out, int32_t n_wave_t,

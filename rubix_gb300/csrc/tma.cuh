@@ -1,5 +1,5 @@
-// Inline-PTX helpers for 1-D TMA bulk copies (cp.async.bulk) completed on a shared
-// memory mbarrier, with bounded waits.
+// Inline-PTX helpers for TMA copies (1-D cp.async.bulk and tiled
+// cp.async.bulk.tensor) completed on a shared memory mbarrier, with bounded waits.
 #pragma once
 
 #include "common.cuh"
@@ -42,6 +42,20 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
           "r"(smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Global -> shared tiled copy of one box of a 3-D tensor map (coordinates innermost
+// first).  The innermost coordinate times the element size must be a multiple of 16
+// bytes; the others may lie outside the tensor, where the box is zero-filled.  `map` is
+// the address of a __grid_constant__ CUtensorMap kernel parameter.
+__device__ __forceinline__ void tensor_copy_3d_g2s(void* dst, const void* map, int c0, int c1,
+                                                   int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2),
+      "r"(smem_addr(bar))
       : "memory");
 }
 

@@ -443,6 +443,17 @@ def psf_forward(cube: torch.Tensor, taps_y, taps_x=None, out=None) -> torch.Tens
     return out
 
 
+def psf_status(device=None) -> int:
+    """Device error word of the TMA-staged PSF: 1 if a staged-row wait ran out since the
+    last read (reading clears it), else 0.  Synchronises the current stream."""
+    import ctypes
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    v = ctypes.c_int(0)
+    _lib.lib().rubix_psf_status(ctypes.byref(v), _stream(dev))
+    return int(v.value)
+
+
 def lsf_forward(cube: torch.Tensor, taps, crop: int, out=None) -> torch.Tensor:
     """Full 1-D convolution along the last axis cropped to [crop, L + crop)."""
     _check_cuda("cube", cube, torch.float32)

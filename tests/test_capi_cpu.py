@@ -72,6 +72,7 @@ def test_abi_version_and_workspace_queries(rubix_lib):
                                 None, None, 3, 2, None, None, 22500, 10, None, 0, 0, None, 3721,
                                 None, 0, None), -1, "null pointer"),
     (lambda h: h.rubix_cube_noalloc_status(None, None), -1, "null pointer"),
+    (lambda h: h.rubix_psf_status(None, None), -1, "null pointer"),
     (lambda h: h.rubix_cube_fwd_dust(None, None, None, None, 6, 221, 1221, None, 3721, None,
                                      None, None, None, 3, 2, None, None, None, None, 22500, 10,
                                      None, 0, 0, None, 3721, None, 0, None), -1,

@@ -225,12 +225,14 @@ def test_renderer_fused_lsf_matches_oracle(ops):
 def test_psf_packed_kernel_equals_scalar_kernel(ops, m):
     """Host taps run the packed two-lane FMA kernel (up to 17 taps), device taps the
     scalar one: same products in the same order, so the cubes are bit-identical; ragged
-    x and wavelength edges and a padded spaxel stride included."""
+    x and wavelength edges and padded spaxel strides included (strides that are a
+    multiple of 4 floats stage the host-tap kernel's rows by TMA)."""
     import torch
 
     rng = np.random.default_rng(m)
     g = rng.uniform(0.1, 1.0, m).astype(np.float32)
-    for ny, nx, L, pad in ((40, 37, 45, 0), (25, 25, 3721, 0), (9, 70, 33, 5)):
+    for ny, nx, L, pad in ((40, 37, 45, 0), (25, 25, 3721, 0), (9, 70, 33, 5),
+                           (40, 37, 45, 3), (25, 25, 3721, 3), (9, 70, 33, 3), (33, 64, 128, 0)):
         base = torch.from_numpy(rng.standard_normal((ny, nx, L + pad)).astype(np.float32)).cuda()
         cube = base[:, :, :L]
         a = ops.psf_forward(cube, g)
@@ -238,4 +240,35 @@ def test_psf_packed_kernel_equals_scalar_kernel(ops, m):
         torch.cuda.synchronize()
         assert torch.equal(a, b), (m, ny, nx, L, pad)
     want = oracle.apply_psf(base[:, :, :L].cpu().numpy().astype(np.float64), np.outer(g, g))
+    np.testing.assert_allclose(a.cpu().numpy(), want, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("m", [1, 5, 15, 17])
+def test_psf_tma_staged_rows_equal_copy_staged_rows(ops, m):
+    """A spaxel stride that is a multiple of 4 floats (16-byte rows) stages the PSF's
+    input rows with tiled TMA copies, any other stride with 4-byte cp.async copies; the
+    arithmetic is the same, so the cubes are bit-identical.  Cases: strips and
+    wavelength tiles cut at the cube's edges (x, y and L not multiples of the 32 x 32
+    tile), fewer rows than the ring holds, and the renderer's padded layout (L = 3721 on
+    a 3724-float stride).  The kernel's device error word stays 0."""
+    import torch
+
+    rng = np.random.default_rng(100 + m)
+    g = rng.uniform(0.1, 1.0, m).astype(np.float32)
+    for ny, nx, L in ((40, 37, 45), (3, 70, 33), (25, 25, 3721), (50, 33, 3721), (1, 1, 7)):
+        Lp = (L + 3) // 4 * 4
+        dense = torch.from_numpy(rng.standard_normal((ny, nx, L)).astype(np.float32)).cuda()
+        pad = torch.full((ny, nx, Lp + 4), float("nan"), device="cuda")  # never read
+        pad[:, :, :L] = dense
+        a = ops.psf_forward(pad[:, :, :L], g)      # 16-byte rows: TMA
+        so = L + 1 if (L + 1) % 4 else L + 2  # not a multiple of 4 floats: cp.async
+        odd = torch.full((ny, nx, so), float("nan"), device="cuda")
+        odd[:, :, :L] = dense
+        b = ops.psf_forward(odd[:, :, :L], g)
+        c = ops.psf_forward(dense, g)              # stride L, L % 4 != 0 here: cp.async
+        torch.cuda.synchronize()
+        assert torch.equal(a, b) and torch.equal(a, c), (m, ny, nx, L)
+        assert not torch.isnan(a).any()
+    assert ops.psf_status() == 0
+    want = oracle.apply_psf(dense.cpu().numpy().astype(np.float64), np.outer(g, g))
     np.testing.assert_allclose(a.cpu().numpy(), want, rtol=1e-5, atol=1e-5)
