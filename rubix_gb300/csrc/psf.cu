@@ -357,14 +357,16 @@ __global__ void __launch_bounds__(kPsfThreads, 2) psf_reg2_kernel(PsfArgs a) {
 // the rest of its strip).  Sticky until rubix_psf_status reads it.
 __device__ int g_psf_error;
 
-// The strip of psf_reg2_kernel with its input rows staged by TMA: thread 0 loads input
+// The strip of psf_reg_body with its input rows staged by TMA: thread 0 loads input
 // row r (W spaxel columns from x0 - (M-1) + ox, kTileL wavelengths from l0, zero outside
 // the cube) with one tiled copy of the 3-D tensor map (wavelength, x, y) into ring slot
 // r % S, completing on that slot's mbarrier, S - 1 rows ahead.  The copies replace the
 // per-thread 4-byte copies, their address arithmetic and validity masks.  The
 // wavelength coordinate l0 is a multiple of 32 floats (128 bytes), as a tiled copy
-// needs; x and y may start outside the cube, where the copy fills zeros.  Same products
-// and summation order as psf_reg2_kernel: bit-identical.
+// needs; x and y may start outside the cube, where the copy fills zeros.  The x-pass
+// runs scalar FMAs on the parameter taps, the y-pass packed FMAs (__ffma2_rn) on tap
+// pairs held in registers.  Same products and summation order as psf_reg_body and
+// psf_reg2_kernel: bit-identical.
 // Ring depth of the TMA-staged kernel: as many staged rows as fit in 48 KB of static
 // shared memory next to the slots' mbarriers, at most 8.
 __host__ __device__ constexpr int psf_tma_stages(int M) {
@@ -379,7 +381,6 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
   constexpr int W = kPsfTileX + M - 1;  // staged row width
   constexpr int kS = psf_tma_stages(M);
   static_assert(kS >= 3, "PSF ring needs at least 3 rows");
-  constexpr int NA = (kPsfXB + M - 1) / 2;  // aligned input pairs per thread and row
   constexpr uint32_t kRowBytes = W * kPsfTileL * sizeof(float);
   static_assert(kPsfXB == 4 && (M & 1), "two output pairs, odd tap count");
   static_assert((W * kPsfTileL * sizeof(float)) % 128 == 0, "ring slots stay 128-byte aligned");
@@ -415,6 +416,15 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
     win[i][0] = make_float2(0.f, 0.f);
     win[i][1] = win[i][0];
   }
+  // y taps as register pairs for the packed FMAs, formed once: made opaque by the move,
+  // so the compiler keeps them instead of re-forming pairs from the parameters per use
+  float2 typ[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    unsigned long long v;
+    asm volatile("mov.b64 %0, {%1, %1};" : "=l"(v) : "f"(a.ty[i]));
+    typ[i] = *reinterpret_cast<const float2*>(&v);
+  }
   for (int r0 = 0; r0 < total; r0 += M) {
 #pragma unroll
     for (int jj = 0; jj < M; ++jj) {
@@ -439,33 +449,29 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
           tensor_copy_3d_g2s(s_in[rn % kS], &map, l0, xsrc0, rn, &s_bar[rn % kS]);
         }
       }
+      // x-pass: scalar FMAs, the taps straight from the kernel parameters
       const float* row = s_in[slot];
-      float2 A[NA], B[NA - 1];
+      float xv[kPsfXB + M - 1];
 #pragma unroll
-      for (int m = 0; m < NA; ++m) {
-        A[m].x = row[(xb + 2 * m) * kPsfTileL + lane];
-        A[m].y = row[(xb + 2 * m + 1) * kPsfTileL + lane];
+      for (int q = 0; q < kPsfXB + M - 1; ++q) xv[q] = row[(xb + q) * kPsfTileL + lane];
+      float hs[kPsfXB];
+#pragma unroll
+      for (int j = 0; j < kPsfXB; ++j) {
+        float v = 0.f;
+#pragma unroll
+        for (int i = 0; i < M; ++i) v = fmaf(a.tx[i], xv[j + (M - 1) - i], v);
+        hs[j] = v;
       }
-#pragma unroll
-      for (int m = 0; m < NA - 1; ++m) B[m] = make_float2(A[m].y, A[m + 1].x);
-      float2 h0 = make_float2(0.f, 0.f), h1 = h0;
-#pragma unroll
-      for (int i = 0; i < M; ++i) {
-        const float2 t = make_float2(a.tx[i], a.tx[i]);
-        const int k0 = M - 1 - i, k1 = M + 1 - i;  // first input of outputs 0-1 and 2-3
-        h0 = __ffma2_rn(t, (k0 & 1) ? B[k0 >> 1] : A[k0 >> 1], h0);
-        h1 = __ffma2_rn(t, (k1 & 1) ? B[k1 >> 1] : A[k1 >> 1], h1);
-      }
-      win[jj][0] = h0;
-      win[jj][1] = h1;
+      win[jj][0] = make_float2(hs[0], hs[1]);
+      win[jj][1] = make_float2(hs[2], hs[3]);
+      // y-pass: packed FMAs over the two output pairs
       const int y = r - oy;
       if (y >= 0 && l < nl) {
         float2 o0 = make_float2(0.f, 0.f), o1 = o0;
 #pragma unroll
         for (int i = 0; i < M; ++i) {
-          const float2 t = make_float2(a.ty[i], a.ty[i]);
-          o0 = __ffma2_rn(t, win[(jj - i + M) % M][0], o0);
-          o1 = __ffma2_rn(t, win[(jj - i + M) % M][1], o1);
+          o0 = __ffma2_rn(typ[i], win[(jj - i + M) % M][0], o0);
+          o1 = __ffma2_rn(typ[i], win[(jj - i + M) % M][1], o1);
         }
         const int x = x0 + xb;
         float* o = out + ((long long)y * nx + x) * sout + l;
