@@ -14,17 +14,17 @@ import bench  # noqa: E402
 
 def test_profile_figures_scale_with_the_particle_count():
     # profiles/cube_fwd_ifu.txt: captured at 1e6 particles, fixed + per-particle parts
-    assert bench.traffic_per_launch(1_000_000) == pytest.approx(390.81e6)
-    assert bench.instructions_per_launch(1_000_000) == pytest.approx(3032.6e6)
+    assert bench.traffic_per_launch(1_000_000) == pytest.approx(390.28e6)
+    assert bench.instructions_per_launch(1_000_000) == pytest.approx(3001.9e6)
     # the 2e5-particle capture lies on the same line
-    assert bench.instructions_per_launch(200_000) == pytest.approx(713.5e6, rel=1e-3)
-    assert bench.traffic_per_launch(200_000) == pytest.approx(305.64e6, rel=2e-3)
+    assert bench.instructions_per_launch(200_000) == pytest.approx(708.5e6, rel=1e-3)
+    assert bench.traffic_per_launch(200_000) == pytest.approx(305.13e6, rel=2e-3)
 
 
 def test_large_grid_profile_reproduces_its_first_capture():
     # profiles/cube_fwd_large.txt: keys from the 2e6 capture; the 1e6 capture lies on the line
-    assert bench.traffic_per_launch(1_000_000, "large") == pytest.approx(1412.12e6, rel=1e-4)
-    assert bench.instructions_per_launch(1_000_000, "large") == pytest.approx(3418.4e6, rel=1e-4)
+    assert bench.traffic_per_launch(1_000_000, "large") == pytest.approx(1417.92e6, rel=1e-4)
+    assert bench.instructions_per_launch(1_000_000, "large") == pytest.approx(3392.6e6, rel=1e-4)
 
 
 def test_profile_figures_need_a_summary_of_the_workload_grid():
