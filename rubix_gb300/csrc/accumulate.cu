@@ -310,8 +310,7 @@ __device__ __forceinline__ void build_plan(const MainArgs& a, const ParticleRec*
 // and stores of a quarter-warp fall in distinct banks.  Every entry is computed with the
 // arithmetic of build_step, so the rows equal build_plan's bit for bit.  Odd kBU keeps a
 // quarter-warp's entries in distinct banks; R = 6 and R = 11 take 5-entry groups, which
-// keep those kernels free of spills.  The dust kernels keep build_plan: next to the transmission
-// state, the group build spills there at any group length.
+// keep those kernels free of spills.
 template <int R>
 constexpr int build_group_len() {
   return (R > 10 || R < 8) ? 5 : 7;
@@ -640,7 +639,9 @@ __global__ void __launch_bounds__(kAccThreads, 2) cube_main_kernel(MainArgs a) {
   const int P = a.pool;
   constexpr bool staged = kStaged;
   constexpr int kBU = build_group_len<R>();
-  constexpr bool kGroups = kStaged && !kDust;  // rows built by groups of kBU entries
+  // rows built by groups of kBU entries (the dust kernel at R = 11 keeps build_plan: the
+  // group build spills 72 bytes there)
+  constexpr bool kGroups = kStaged && (!kDust || R <= 10);
   float lam[R], acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {

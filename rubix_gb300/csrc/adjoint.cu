@@ -163,6 +163,98 @@ __device__ __forceinline__ void adj_build(const AdjArgs& a, const ParticleRec& r
   }
 }
 
+constexpr int kAdjBU = 3;
+// Grouped build: thread g builds entries [g*kAdjBU, (g+1)*kAdjBU) of the particle's two
+// rows from kAdjBU + 1 positions of its own (no shuffles), so an ~800-entry row takes one
+// round of ~270 threads instead of two or three 31-entry warp steps per warp.  Staged rows
+// touching neither grid end (kstart >= 0, kend + 1 <= nW - 1) need no clamps; the others
+// take adj_build's per-entry arithmetic.  Same operations per entry as adj_build:
+// identical rows.
+__device__ __forceinline__ void adj_build_groups(const AdjArgs& a, const ParticleRec& r,
+                                                 const float* __restrict__ s_wz, float4 wt,
+                                                 float4 dw, const float4* __restrict__ stage,
+                                                 float4* __restrict__ row_a,
+                                                 float4* __restrict__ row_b, int tid) {
+  const int nW = a.n_wave;
+  const float alpha = r.a.y;
+  const int ks = r.b.y, ke = r.b.z & ~kGenericFlag;
+  const int klo = max(ks, 0), khi = min(ke + 1, nW - 1);
+  const int n_e = ke - ks + 1;
+  const int cell = r.b.x;
+  const bool has_cell = cell >= 0;
+  // staged only: the loads of a partial last group run up to 2 entries past the row,
+  // which stays inside the staging buffer (n_wave + 2 entries) and shared memory
+  const bool plain = a.staged && ks >= 0 && ke + 1 <= nW - 1;
+  const float4* st = a.staged ? stage - klo : a.ct + (long long)max(cell, 0) * nW;
+  for (int e0 = tid * kAdjBU; e0 < n_e; e0 += kAdjThreads * kAdjBU) {
+    const int k0 = ks + e0;
+    if (plain) {
+      float G[kAdjBU + 1], GZ[kAdjBU + 1], GA[kAdjBU + 1], lp[kAdjBU + 1];
+#pragma unroll
+      for (int j = 0; j <= kAdjBU; ++j) {
+        float g = 0.f, gz = 0.f, ga = 0.f;
+        const float4 c = st[k0 + j];
+        if (has_cell) {
+          g = wt.x * c.x;
+          g = fmaf(wt.y, c.y, g);
+          g = fmaf(wt.z, c.z, g);
+          g = fmaf(wt.w, c.w, g);
+          gz = fmaf(dw.x, c.y - c.x, dw.y * (c.w - c.z));
+          ga = fmaf(dw.z, c.z - c.x, dw.w * (c.w - c.y));
+        }
+        G[j] = g;
+        GZ[j] = gz;
+        GA[j] = ga;
+        lp[j] = __fmul_rn(s_wz[k0 + j], alpha);
+      }
+#pragma unroll
+      for (int j = 0; j < kAdjBU; ++j) {
+        const float dl = lp[j + 1] - lp[j];
+        const float inv = dl > 0.f ? __fdividef(1.f, dl) : 0.f;
+        if (e0 + j < n_e) {
+          row_a[e0 + j] = make_float4(lp[j], (G[j + 1] - G[j]) * inv, G[j], lp[j + 1]);
+          row_b[e0 + j] = make_float4(GZ[j], (GZ[j + 1] - GZ[j]) * inv, GA[j],
+                                      (GA[j + 1] - GA[j]) * inv);
+        }
+      }
+    } else {
+      for (int j = 0; j < kAdjBU; ++j) {
+        const int e = e0 + j;
+        if (e >= n_e) break;
+        float G2[2], GZ2[2], GA2[2], lp2[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int k = ks + e + q;
+          const int kk = min(max(k, klo), khi);
+          float g = 0.f, gz = 0.f, ga = 0.f;
+          if (has_cell) {
+            const float4 c = st[kk];
+            g = wt.x * c.x;
+            g = fmaf(wt.y, c.y, g);
+            g = fmaf(wt.z, c.z, g);
+            g = fmaf(wt.w, c.w, g);
+            gz = fmaf(dw.x, c.y - c.x, dw.y * (c.w - c.z));
+            ga = fmaf(dw.z, c.z - c.x, dw.w * (c.w - c.y));
+          }
+          G2[q] = g;
+          GZ2[q] = gz;
+          GA2[q] = ga;
+          lp2[q] = (k < 0) ? -kFltMax : (k >= nW ? kFltMax : __fmul_rn(s_wz[k], alpha));
+        }
+        const int k = ks + e;
+        float inv = 0.f;
+        if (k >= 0 && k + 1 < nW) {
+          const float dl = lp2[1] - lp2[0];
+          inv = dl > 0.f ? __fdividef(1.f, dl) : 0.f;
+        }
+        const float lpw = (k + 1 >= nW) ? kFltMax : lp2[1];
+        row_a[e] = make_float4(lp2[0], (G2[1] - G2[0]) * inv, G2[0], lpw);
+        row_b[e] = make_float4(GZ2[0], (GZ2[1] - GZ2[0]) * inv, GA2[0], (GA2[1] - GA2[0]) * inv);
+      }
+    }
+  }
+}
+
 // One-step walk on the two row arrays, branch-free: if x >= e.w advance both entry
 // addresses by one and load both next entries (predicated add and loads).
 __device__ __forceinline__ void walk_step2(float x, unsigned& aa, unsigned& ab, float4& e,
@@ -350,7 +442,11 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
         if (!mbar_wait_bounded(&s_bar, phase)) s_fail = 1;
         phase ^= 1u;
       }
-      adj_build(a, rec, wzp, s_wt[buf][0], s_wt[buf][1], s_stage, s_ra, s_rb, lane, warp);
+      // the dust kernels and R = 11 keep the warp-step build, which does not spill there
+      if constexpr (!kDust && R <= 10)
+        adj_build_groups(a, rec, wzp, s_wt[buf][0], s_wt[buf][1], s_stage, s_ra, s_rb, tid);
+      else
+        adj_build(a, rec, wzp, s_wt[buf][0], s_wt[buf][1], s_stage, s_ra, s_rb, lane, warp);
       __syncthreads();  // rows ready; staging consumed
       if (s_fail) {
         if (tid == 0) {
@@ -387,7 +483,10 @@ __global__ void __launch_bounds__(kAdjThreads, 2) cube_adjoint_kernel(AdjArgs a)
         if (lane == 0) s_red_av[buf][warp] = sav;
       }
       __syncthreads();  // partial sums visible; rows free for the next particle
-      if (warp == 0) {
+      // the last warp finalises: its share of the next row build is the smallest (groups
+      // fill the warps in order; warp steps give the extra steps to the first warps),
+      // and thread 0 issues the next particle's copy
+      if (warp == kAdjWarps - 1) {
         // lane l: value l & 7 over warps (l >> 3), (l >> 3) + 4, (l >> 3) + 8 (independent
         // loads), then over the four lane groups; fixed order, so deterministic
         const float* red = s_red + buf * kAdjWarps * kAdjSums;
