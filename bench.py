@@ -80,17 +80,40 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def fp32_peak_tflops(dev, reps=5):
-    """FP32 FMA rate of this GPU from the library's FMA-chain probe (best of reps)."""
+def fma_probe(dev, iters: int = 4096):
+    """(FMAs launched, out tensor): one launch of the FP32 FMA-rate probe
+    (bench_fma_probe.cu, built by rubix_gb300._build.build_probe into its own library)
+    on the current stream."""
+    import ctypes
+
     import torch
 
-    from rubix_gb300 import ops
+    from rubix_gb300 import _build
+
+    lib = ctypes.CDLL(_build.build_probe())
+    lib.rubix_probe_fma_blocks.restype = ctypes.c_int
+    lib.rubix_probe_fma.restype = ctypes.c_int
+    lib.rubix_probe_fma.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+    blocks = lib.rubix_probe_fma_blocks()
+    if blocks <= 0:
+        raise RuntimeError("rubix_probe_fma_blocks failed")
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
+    rc = lib.rubix_probe_fma(ctypes.c_void_p(out.data_ptr()), int(iters),
+                             ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    if rc != 0:
+        raise RuntimeError(f"rubix_probe_fma returned {rc}")
+    return blocks * 256 * int(iters) * 128, out
+
+
+def fp32_peak_tflops(dev, reps=5):
+    """FP32 FMA rate of this GPU from the FMA-chain probe (best of reps)."""
+    import torch
 
     best = 0.0
     for i in range(reps + 2):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        n_fma, _ = ops.fma_probe(dev)
+        n_fma, _ = fma_probe(dev)
         e1.record()
         torch.cuda.synchronize()
         if i >= 2:
@@ -1128,7 +1151,7 @@ def main():
     fp32_peak = fp32_peak_tflops(dev)
     fp32_achieved = fpl * N * L / cube_avg_s / 1e12
     compute = {"fp32_peak_tflops": fp32_peak, "peak_source": "measured FMA-chain probe "
-               "(rubix_fma_probe)", "achieved_tflops": fp32_achieved,
+               "(bench_fma_probe.cu)", "achieved_tflops": fp32_achieved,
                "frac": fp32_achieved / fp32_peak if fp32_peak else None,
                "flops_per_particle_lambda": fpl}
     # instruction issue, the resource the main kernel is bound by: warp instructions per

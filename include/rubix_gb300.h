@@ -327,16 +327,6 @@ RUBIX_API int rubix_lsf_fwd_dtaps(const float* in, float* out, int64_t n_rows,
 RUBIX_API int rubix_gauss_taps(const double* sigma, const double* x, int32_t m, float* taps,
                                float* dtaps, float* rtaps, int32_t rtaps_pad, void* stream);
 
-/*
- * No counterpart in rubix (a measurement aid).
- *
- * rubix_fma_probe_blocks() blocks of 256 threads each run iters * 128 dependent-chain
- * FP32 FMAs (8 chains per thread) and store one float per thread into out
- * (rubix_fma_probe_blocks() * 256 floats): timing a launch gives the FP32 FMA rate
- * against which the compute roofline of the kernels is stated.
- */
-RUBIX_API int rubix_fma_probe_blocks(void);
-RUBIX_API int rubix_fma_probe(float* out, int32_t iters, void* stream);
 
 /*
  * No counterpart in rubix (rubix has no C interface; JAX allocates its buffers).

@@ -19,6 +19,9 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OBJDIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "librubix_gb300.so")
+# bench-only measurement aid (the FP32 FMA-rate probe), kept out of the product library
+PROBE_SRC = os.path.join(ROOT, "bench_fma_probe.cu")
+PROBE_PATH = os.path.join(HERE, "librubix_gb300_probe.so")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -93,5 +96,21 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB_PATH
 
 
+def build_probe(force: bool = False) -> str:
+    """Compile bench.py's FP32 FMA-rate probe into its own small library (not part of
+    librubix_gb300) if needed and return its path."""
+    if (not force and os.path.exists(PROBE_PATH)
+            and os.path.getmtime(PROBE_PATH) >= os.path.getmtime(PROBE_SRC)):
+        return PROBE_PATH
+    tmp = PROBE_PATH + ".tmp"
+    cmd = [_nvcc(), *ARCH_FLAGS, *NVCC_FLAGS, "-shared", PROBE_SRC, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {PROBE_SRC}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, PROBE_PATH)
+    return PROBE_PATH
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_probe(force="--force" in sys.argv))

@@ -61,8 +61,6 @@ SIGNATURES = {
     "rubix_lsf_fwd_dtaps": (_c.c_int, [_vp, _vp, _i64, _i32, _i64, _i64, _vp, _i32, _i32,
                                        _vp]),
     "rubix_gauss_taps": (_c.c_int, [_vp, _vp, _i32, _vp, _vp, _vp, _i32, _vp]),
-    "rubix_fma_probe_blocks": (_c.c_int, []),
-    "rubix_fma_probe": (_c.c_int, [_vp, _i32, _vp]),
     "rubix_dust_av_workspace_size": (_sz, [_i64, _i32]),
     "rubix_dust_av": (_c.c_int, [_vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _i32,
                                  _vp, _vp, _sz, _vp]),

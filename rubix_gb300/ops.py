@@ -709,15 +709,5 @@ def gauss_taps(sigma: torch.Tensor, x, reversed_pad: bool = False):
     return taps, dtaps, rtaps
 
 
-def fma_probe(device, iters: int = 4096):
-    """(FMAs launched, out tensor): one launch of the FP32 FMA-rate probe on the current
-    stream; time it with CUDA events to get the FMA rate."""
-    blocks = int(_lib.lib().rubix_fma_probe_blocks())
-    out = torch.empty(blocks * 256, dtype=torch.float32, device=device)
-    _lib.call("rubix_fma_probe", _ptr(out), int(iters), _stream(torch.device(device)))
-    _count(1)
-    return blocks * 256 * int(iters) * 128, out
-
-
 def _key_passes(max_key: int) -> int:
     return (max(int(max_key), 0).bit_length() + 7) // 8

@@ -86,7 +86,6 @@ def test_abi_version_and_workspace_queries(rubix_lib):
     (lambda h: h.rubix_fits_cube_layout(None, 4, 70000, 8, 8, None, None), -2,
      "65535 columns"),
     (lambda h: h.rubix_fits_cube_layout(None, 4, 4, 8, 4, None, None), -2, "spaxel_stride"),
-    (lambda h: h.rubix_fma_probe(None, 10, None), -1, "bad arguments"),
     (lambda h: h.rubix_orient_filter_assign(None, None, 10, None, None, None, None, 1, 0, None,
                                             None, None, None, None, None), -2, "two edges"),
     (lambda h: h.rubix_orient_filter_assign(None, None, 10, None, None, None, None, 26, 9, None,

@@ -134,13 +134,17 @@ def test_capi_rejects_bad_arguments():
 
 
 def test_fma_probe_runs():
-    """The FP32 rate probe launches, writes one finite value per thread and reports its
-    FMA count."""
+    """bench.py's FP32 rate probe (a bench-only library) launches, writes one finite value
+    per thread and reports its FMA count."""
+    import os
+    import sys
+
     import torch
 
-    from rubix_gb300 import ops
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
 
-    n_fma, out = ops.fma_probe("cuda", iters=8)
+    n_fma, out = bench.fma_probe("cuda", iters=8)
     torch.cuda.synchronize()
     assert n_fma == out.numel() * 8 * 128
     assert torch.isfinite(out).all()
