@@ -503,6 +503,29 @@ RUBIX_API size_t rubix_dot_workspace_size(void);
 RUBIX_API int rubix_dot(const float* a, const float* b, int64_t n, double* out, void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/*
+ * No counterpart in rubix (jax.grad forms these inner products inside XLA).
+ * Fused forms of rubix_dot(w, conv(in)) for the σ gradients, the convolution never
+ * written to memory: *out (device double) = sum over the cube of w * PSF(in) with the
+ * device taps ty (y) and tx (x) of rubix_psf_fwd_dtaps (m odd, <= 21), or
+ * sum over rows of w * LSF(in) with the device taps of rubix_lsf_fwd_dtaps
+ * (n_taps <= 28).  The convolution is computed with the same arithmetic as those
+ * entry points; per-thread float partial sums, double block sums added in block order
+ * (deterministic).  The workspace (rubix_fused_dot_workspace_size bytes, 8-byte
+ * aligned) must not be shared by calls in flight at the same time.  Other tap counts
+ * return RUBIX_E_UNSUPPORTED.
+ */
+RUBIX_API size_t rubix_fused_dot_workspace_size(void);
+RUBIX_API int rubix_psf_dot_dtaps(const float* in, int64_t spaxel_stride_in, const float* w,
+                                  int64_t spaxel_stride_w, int32_t ny, int32_t nx,
+                                  int32_t n_wave_t, const float* ty, const float* tx, int32_t m,
+                                  double* out, void* workspace, size_t workspace_bytes,
+                                  void* stream);
+RUBIX_API int rubix_lsf_dot_dtaps(const float* in, int64_t n_rows, int32_t n_wave_t,
+                                  int64_t row_stride_in, const float* w, int64_t row_stride_w,
+                                  const float* taps, int32_t n_taps, int32_t crop, double* out,
+                                  void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Ragged batches of galaxies                                                */
 /* ------------------------------------------------------------------------- */

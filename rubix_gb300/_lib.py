@@ -82,6 +82,13 @@ SIGNATURES = {
         _c.c_int, [_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _vp, _i32, _vp]
     ),
     "rubix_psf_status": (_c.c_int, [_c.POINTER(_c.c_int), _vp]),
+    "rubix_fused_dot_workspace_size": (_sz, []),
+    "rubix_psf_dot_dtaps": (
+        _c.c_int, [_vp, _i64, _vp, _i64, _i32, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _sz, _vp]
+    ),
+    "rubix_lsf_dot_dtaps": (
+        _c.c_int, [_vp, _i64, _i32, _i64, _vp, _i64, _vp, _i32, _i32, _vp, _vp, _sz, _vp]
+    ),
     "rubix_lsf_fwd": (_c.c_int, [_vp, _vp, _i64, _i32, _i64, _i64, _vp, _i32, _i32, _vp]),
     "rubix_cube_bwd_workspace_size": (_sz, [_i64, _i32, _i32, _i32, _i32, _i32]),
     "rubix_cube_bwd": (

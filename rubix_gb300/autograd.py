@@ -159,10 +159,18 @@ class DatacubeFunction(torch.autograd.Function):
                 grads[3] = gvel
         if need[4]:
             Qc = Q.view(r.sbin, r.sbin, -1)
-            d = ops.dot(g, ops.psf_forward(Qc, dtp, tp)) + ops.dot(g, ops.psf_forward(Qc, tp, dtp))
+            if tp.numel() <= 21 and tp.numel() % 2 == 1:
+                # <g, PSF(Q)> fused: the two convolutions are never written
+                d = ops.psf_dot(Qc, dtp, tp, g) + ops.psf_dot(Qc, tp, dtp, g)
+            else:
+                d = (ops.dot(g, ops.psf_forward(Qc, dtp, tp))
+                     + ops.dot(g, ops.psf_forward(Qc, tp, dtp)))
             grads[4] = d.to(ctx.sigma_dtypes[0] or torch.float32)
         if need[5]:
-            d = ops.dot(gP.view(nseg, -1), ops.lsf_forward(A, dtl, crop))
+            if dtl.numel() <= 28:
+                d = ops.lsf_dot(A, dtl, crop, gP.view(nseg, -1))
+            else:
+                d = ops.dot(gP.view(nseg, -1), ops.lsf_forward(A, dtl, crop))
             grads[5] = d.to(ctx.sigma_dtypes[1] or torch.float32)
         return tuple(grads)
 

@@ -14,6 +14,7 @@
 // with a single tiled TMA copy (psf_tma_kernel); otherwise every thread issues 4-byte
 // cp.async copies of its share of the row.
 #include "common.cuh"
+#include "dot_reduce.cuh"
 #include "tma.cuh"
 
 #include <cuda.h>  // CUtensorMap and its enums; cuTensorMapEncodeTiled comes through the runtime
@@ -128,12 +129,15 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // The strip (bx, by) of one cube: ny x nx spaxels (spaxel strides sin/sout), nl
 // wavelengths, taps ty/tx (M each, any address space), 'same' offsets oy/ox.
-template <int M>
+// kDot: instead of storing an output o[y][x][l], add w[y][x][l] * o to `dot` (w has
+// the output's layout, spaxel stride sout); `out` is not written.
+template <int M, bool kDot = false>
 __device__ __forceinline__ void psf_reg_body(const float* __restrict__ in, float* __restrict__ out,
                                              int ny, int nx, int nl, long long sin,
                                              long long sout, int oy, int ox,
                                              const float* ty_src, const float* tx_src, int bx,
-                                             int by) {
+                                             int by, const float* __restrict__ w = nullptr,
+                                             float* dot = nullptr) {
   constexpr int W = kPsfTileX + M - 1;  // staged row width
   constexpr int PER = (W * kPsfTileL + kPsfThreads - 1) / kPsfThreads;
   constexpr int kPsfStages = psf_stages(M);
@@ -204,6 +208,16 @@ __device__ __forceinline__ void psf_reg_body(const float* __restrict__ in, float
         cp_async_commit();
       }
       const float* row = s_in[r % kPsfStages];
+      // dot mode: this row's weights, loaded now so the x-pass hides their latency
+      float wv[kPsfXB];
+      if constexpr (kDot) {
+        const int yw = r - oy;
+#pragma unroll
+        for (int j = 0; j < kPsfXB; ++j) {
+          const int x = x0 + xb + j;
+          wv[j] = (yw >= 0 && l < nl && x < nx) ? w[((long long)yw * nx + x) * sout + l] : 0.f;
+        }
+      }
       // x-pass over the staged row r for this thread's kPsfXB positions
       float xv[kPsfXB + M - 1];
 #pragma unroll
@@ -224,7 +238,11 @@ __device__ __forceinline__ void psf_reg_body(const float* __restrict__ in, float
 #pragma unroll
           for (int i = 0; i < M; ++i) o = fmaf(ty[i], win[(jj - i + M) % M][j], o);
           const int x = x0 + xb + j;
-          if (x < nx) out[((long long)y * nx + x) * sout + l] = o;
+          if constexpr (kDot) {
+            *dot = fmaf(wv[j], o, *dot);  // wv[j] = 0 outside the cube
+          } else {
+            if (x < nx) out[((long long)y * nx + x) * sout + l] = o;
+          }
         }
       }
     }
@@ -237,6 +255,19 @@ __global__ void __launch_bounds__(kPsfThreads) psf_reg_kernel(PsfArgs a) {
   psf_reg_body<M>(a.in, a.out, a.ny, a.nx, a.nl, a.sin, a.sout, a.oy, a.ox,
                   a.ty_dev ? a.ty_dev : a.ty, a.tx_dev ? a.tx_dev : a.tx, blockIdx.x,
                   blockIdx.y);
+}
+
+// sum over the cube of w * PSF(in), the PSF with device taps (psf_reg_body's arithmetic
+// per output), reduced deterministically; the PSF output is never written.
+template <int M>
+__global__ void __launch_bounds__(kPsfThreads) psf_dot_kernel(PsfArgs a, const float* w,
+                                                             FusedDotScratch* ws, double* out) {
+  __shared__ double s_w[kPsfThreads / 32];
+  __shared__ int s_last;
+  float dot = 0.f;
+  psf_reg_body<M, true>(a.in, nullptr, a.ny, a.nx, a.nl, a.sin, a.sout, a.oy, a.ox, a.ty_dev,
+                        a.tx_dev, blockIdx.x, blockIdx.y, w, &dot);
+  fused_dot_finish(dot, ws, out, s_w, &s_last);
 }
 
 // The same strip with packed two-lane FMAs (__ffma2_rn) for host taps: the four x
@@ -666,6 +697,75 @@ extern "C" int rubix_psf_fwd_dtaps(const float* in, float* out, int32_t ny, int3
                                    const float* tx, int32_t m_x, void* stream) {
   return psf_fwd_impl(in, out, ny, nx, n_wave_t, spaxel_stride_in, spaxel_stride_out, ty, m_y,
                       tx, m_x, true, stream);
+}
+
+extern "C" size_t rubix_fused_dot_workspace_size(void) { return sizeof(FusedDotScratch); }
+
+extern "C" int rubix_psf_dot_dtaps(const float* in, int64_t spaxel_stride_in, const float* w,
+                                   int64_t spaxel_stride_w, int32_t ny, int32_t nx,
+                                   int32_t n_wave_t, const float* ty, const float* tx, int32_t m,
+                                   double* out, void* workspace, size_t workspace_bytes,
+                                   void* stream) {
+  RUBIX_REQUIRE(ny >= 0 && nx >= 0 && n_wave_t >= 0, RUBIX_E_SHAPE,
+                "rubix_psf_dot_dtaps: negative size");
+  RUBIX_REQUIRE(m >= 1 && m <= 21 && (m & 1), RUBIX_E_UNSUPPORTED,
+                "rubix_psf_dot_dtaps: tap count must be odd and <= 21, got %d", m);
+  RUBIX_REQUIRE(spaxel_stride_in >= n_wave_t && spaxel_stride_w >= n_wave_t, RUBIX_E_SHAPE,
+                "rubix_psf_dot_dtaps: spaxel stride smaller than n_wave_t");
+  RUBIX_REQUIRE((long long)nx * spaxel_stride_in < (1LL << 31), RUBIX_E_SHAPE,
+                "rubix_psf_dot_dtaps: rows too long");
+  RUBIX_REQUIRE(out != nullptr, RUBIX_E_INVALID, "rubix_psf_dot_dtaps: null output");
+  RUBIX_REQUIRE(workspace != nullptr && workspace_bytes >= sizeof(FusedDotScratch) &&
+                    (reinterpret_cast<uintptr_t>(workspace) & 7) == 0,
+                RUBIX_E_WORKSPACE,
+                "rubix_psf_dot_dtaps: workspace of %zu bytes (8-byte aligned) needed",
+                sizeof(FusedDotScratch));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (ny == 0 || nx == 0 || n_wave_t == 0) {
+    RUBIX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double), st));
+    return RUBIX_OK;
+  }
+  RUBIX_REQUIRE(in && w && ty && tx, RUBIX_E_INVALID, "rubix_psf_dot_dtaps: null pointer");
+  const dim3 grid(div_up(nx, kPsfTileX), div_up(n_wave_t, kPsfTileL));
+  RUBIX_REQUIRE((long long)grid.x * grid.y <= kFusedDotMaxBlocks, RUBIX_E_SHAPE,
+                "rubix_psf_dot_dtaps: cube too large (%u x %u strips > %d)", grid.x, grid.y,
+                kFusedDotMaxBlocks);
+  PsfArgs a;
+  a.in = in;
+  a.out = nullptr;
+  a.ny = ny;
+  a.nx = nx;
+  a.nl = n_wave_t;
+  a.sin = spaxel_stride_in;
+  a.sout = spaxel_stride_w;
+  a.my = a.mx = m;
+  a.oy = a.ox = (m - 1) / 2;
+  a.ty_dev = ty;
+  a.tx_dev = tx;
+  auto* scratch = static_cast<FusedDotScratch*>(workspace);
+  RUBIX_CUDA_TRY(cudaMemsetAsync(&scratch->counter, 0, sizeof(unsigned), st));
+  switch (m) {
+#define RUBIX_PSF_DOT(MM)                                                   \
+  case MM:                                                                  \
+    psf_dot_kernel<MM><<<grid, kPsfThreads, 0, st>>>(a, w, scratch, out);   \
+    break;
+    RUBIX_PSF_DOT(1)
+    RUBIX_PSF_DOT(3)
+    RUBIX_PSF_DOT(5)
+    RUBIX_PSF_DOT(7)
+    RUBIX_PSF_DOT(9)
+    RUBIX_PSF_DOT(11)
+    RUBIX_PSF_DOT(13)
+    RUBIX_PSF_DOT(15)
+    RUBIX_PSF_DOT(17)
+    RUBIX_PSF_DOT(19)
+    RUBIX_PSF_DOT(21)
+#undef RUBIX_PSF_DOT
+    default:
+      break;
+  }
+  RUBIX_LAUNCH_CHECK("psf_dot_kernel");
+  return RUBIX_OK;
 }
 
 extern "C" int rubix_psf_status(int* device_error, void* stream) {

@@ -269,6 +269,58 @@ def dot(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def psf_dot(cube: torch.Tensor, taps_y: torch.Tensor, taps_x: torch.Tensor,
+            w: torch.Tensor) -> torch.Tensor:
+    """sum(w * psf_forward(cube, taps_y, taps_x)) as a 0-d float64 device tensor, the
+    convolution never written (device taps, odd count <= 21; the same arithmetic per
+    element as psf_forward with device taps, a deterministic fixed-order sum)."""
+    _check_cuda("cube", cube, torch.float32)
+    _check_cuda("w", w, torch.float32)
+    if cube.dim() != 3 or cube.stride(2) != 1 or cube.stride(0) != cube.shape[1] * cube.stride(1):
+        cube = cube.contiguous()
+    if w.shape != cube.shape:
+        raise ValueError("psf_dot: w must have the cube's shape")
+    if w.stride(2) != 1 or w.stride(0) != w.shape[1] * w.stride(1):
+        w = w.contiguous()
+    ny, nx, L = cube.shape
+    ty = _contig("taps_y", taps_y, torch.float32).reshape(-1)
+    tx = _contig("taps_x", taps_x, torch.float32).reshape(-1)
+    if ty.numel() != tx.numel():
+        raise ValueError("psf_dot: taps_y and taps_x must have the same length")
+    out = torch.empty((), dtype=torch.float64, device=cube.device)
+    ws = workspace(_lib.query("rubix_fused_dot_workspace_size"), cube.device)
+    _lib.call("rubix_psf_dot_dtaps", _ptr(cube), cube.stride(1), _ptr(w), w.stride(1), ny, nx,
+              L, _ptr(ty), _ptr(tx), ty.numel(), _ptr(out), _ptr(ws), ws.numel(),
+              _stream(cube.device))
+    _count(1)
+    return out
+
+
+def lsf_dot(cube: torch.Tensor, taps: torch.Tensor, crop: int, w: torch.Tensor) -> torch.Tensor:
+    """sum(w * lsf_forward(cube, taps, crop)) over rows [..., L] as a 0-d float64 device
+    tensor, the convolution never written (device taps, at most 28; the arithmetic of
+    lsf_forward per element, a deterministic fixed-order sum)."""
+    _check_cuda("cube", cube, torch.float32)
+    _check_cuda("w", w, torch.float32)
+    L = cube.shape[-1]
+    rows = cube.reshape(-1, L)
+    if rows.stride(1) != 1:
+        rows = rows.contiguous()
+    wr = w.reshape(-1, L)
+    if wr.shape != rows.shape:
+        raise ValueError("lsf_dot: w must have the cube's shape")
+    if wr.stride(1) != 1:
+        wr = wr.contiguous()
+    t = _contig("taps", taps, torch.float32).reshape(-1)
+    out = torch.empty((), dtype=torch.float64, device=cube.device)
+    ws = workspace(_lib.query("rubix_fused_dot_workspace_size"), cube.device)
+    _lib.call("rubix_lsf_dot_dtaps", _ptr(rows), rows.shape[0], L, rows.stride(0), _ptr(wr),
+              wr.stride(0), _ptr(t), t.numel(), int(crop), _ptr(out), _ptr(ws), ws.numel(),
+              _stream(cube.device))
+    _count(1)
+    return out
+
+
 def inertia_tensor(coords: torch.Tensor, mass: torch.Tensor, halfmass_radius: float) -> torch.Tensor:
     """[3, 3] float64 moment-of-inertia tensor of the particles within the radius, with
     rubix's index padding (particle 0 once more per particle outside)."""

@@ -73,6 +73,14 @@ def test_abi_version_and_workspace_queries(rubix_lib):
                                 None, 0, None), -1, "null pointer"),
     (lambda h: h.rubix_cube_noalloc_status(None, None), -1, "null pointer"),
     (lambda h: h.rubix_psf_status(None, None), -1, "null pointer"),
+    (lambda h: h.rubix_psf_dot_dtaps(None, 8, None, 8, 4, 4, 8, None, None, 15, None, None, 0,
+                                     None), -1, "null output"),
+    (lambda h: h.rubix_psf_dot_dtaps(None, 8, None, 8, 4, 4, 8, None, None, 23, None, None, 0,
+                                     None), -6, "odd and <= 21"),
+    (lambda h: h.rubix_lsf_dot_dtaps(None, 4, 8, 8, None, 8, None, 40, 0, None, None, 0, None),
+     -6, "n_taps must be in"),
+    (lambda h: h.rubix_lsf_dot_dtaps(None, 4, 8, 8, None, 8, None, 5, 2, None, None, 0, None),
+     -1, "null output"),
     (lambda h: h.rubix_cube_fwd_dust(None, None, None, None, 6, 221, 1221, None, 3721, None,
                                      None, None, None, 3, 2, None, None, None, None, 22500, 10,
                                      None, 0, 0, None, 3721, None, 0, None), -1,

@@ -272,3 +272,47 @@ def test_psf_tma_staged_rows_equal_copy_staged_rows(ops, m):
     assert ops.psf_status() == 0
     want = oracle.apply_psf(dense.cpu().numpy().astype(np.float64), np.outer(g, g))
     np.testing.assert_allclose(a.cpu().numpy(), want, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("m", [1, 7, 15, 21])
+def test_psf_dot_equals_dot_of_psf(ops, m):
+    """<w, PSF(cube)> fused (the convolution never written) against psf_forward followed
+    by the dot product, with device taps, unequal x and y taps, ragged strips and
+    wavelength tiles and a padded spaxel stride: the convolutions are the same float32
+    numbers, only the order of the float64-finished sum differs."""
+    import torch
+
+    rng = np.random.default_rng(200 + m)
+    ty = torch.from_numpy(rng.uniform(0.1, 1.0, m).astype(np.float32)).cuda()
+    tx = torch.from_numpy(rng.uniform(-0.5, 1.0, m).astype(np.float32)).cuda()
+    for ny, nx, L, pad in ((50, 50, 3721, 0), (9, 70, 33, 3), (40, 37, 45, 0)):
+        base = torch.from_numpy(rng.standard_normal((ny, nx, L + pad)).astype(np.float32)).cuda()
+        cube = base[:, :, :L]
+        w = torch.from_numpy(rng.standard_normal((ny, nx, L)).astype(np.float32)).cuda()
+        got = ops.psf_dot(cube, ty, tx, w)
+        want = ops.dot(w, ops.psf_forward(cube, ty, tx))
+        torch.cuda.synchronize()
+        g, v = float(got), float(want)
+        scale = float(w.abs().sum()) * float(ops.psf_forward(cube, ty, tx).abs().max())
+        assert abs(g - v) <= 1e-6 * scale, (m, ny, nx, L, g, v)
+
+
+@pytest.mark.parametrize("k", [3, 13, 28])
+def test_lsf_dot_equals_dot_of_lsf(ops, k):
+    """<w, LSF(rows)> fused against lsf_forward followed by the dot product (device taps,
+    a padded row stride included)."""
+    import torch
+
+    rng = np.random.default_rng(300 + k)
+    taps = torch.from_numpy(rng.uniform(0.05, 1.0, k).astype(np.float32)).cuda()
+    crop = (k - 1) // 2
+    for rows, L, pad in ((2500, 3721, 0), (37, 45, 3)):
+        base = torch.from_numpy(rng.standard_normal((rows, L + pad)).astype(np.float32)).cuda()
+        a = base[:, :L]
+        w = torch.from_numpy(rng.standard_normal((rows, L)).astype(np.float32)).cuda()
+        got = ops.lsf_dot(a, taps, crop, w)
+        conv = ops.lsf_forward(a, taps, crop)
+        want = ops.dot(w, conv)
+        torch.cuda.synchronize()
+        scale = float(w.abs().sum()) * float(conv.abs().max())
+        assert abs(float(got) - float(want)) <= 1e-6 * scale, (k, rows, L)
