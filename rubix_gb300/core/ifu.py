@@ -186,7 +186,7 @@ def get_doppler_shift_and_resampling(config: dict) -> Callable:
     return doppler_shift_and_resampling
 
 
-def get_calculate_datacube(config: dict, lsf_handoff=None) -> Callable:
+def get_calculate_datacube(config: dict, lsf_handoff=None, psf_follows: bool = False) -> Callable:
     """rubix/core/ifu.py:298-341: per-spaxel sum into a [sbin, sbin, n_lambda] cube.
 
     With lazy spectra the fused kernel runs (stable spaxel sort + lookup/mass/Doppler/
@@ -194,7 +194,10 @@ def get_calculate_datacube(config: dict, lsf_handoff=None) -> Callable:
     Particles outside the aperture (zero mass after ``filter_particles``) contribute
     exactly 0 and are left out of the sort.  With ``lsf_handoff`` (a
     ``core.lsf.LsfHandoff`` shared with the run's ``convolve_lsf``) the fused kernel
-    also applies the LSF, and the later ``convolve_lsf`` passes the cube through.
+    also applies the LSF, and the later ``convolve_lsf`` passes the cube through.  With
+    ``psf_follows`` (the pipeline runs ``convolve_psf`` next) the cube is written with a
+    spaxel stride of n_lambda rounded up to a multiple of 4, which lets the PSF stage its
+    rows by TMA; ``convolve_psf`` then replaces it with its dense output.
     """
     logger = get_logger(config.get("logger", None))
     telescope = get_telescope(config)
@@ -218,12 +221,19 @@ def get_calculate_datacube(config: dict, lsf_handoff=None) -> Callable:
             lsf_handoff.pending = fuse
         if lazy:
             flux, zg, ag, _ = spec.ssp.device_arrays(dev)
+            out = None
+            if psf_follows:
+                # 16-byte spaxel rows, so convolve_psf stages them by TMA; the PSF step
+                # replaces this cube with its dense output
+                L = int(spec.wave_t.numel())
+                out = torch.empty((nseg, (L + 3) // 4 * 4), dtype=torch.float32,
+                                  device=dev)[:, :L]
             cube = ops.cube_forward(flux, zg, ag, spec.wave_z, spec.wave_t, spec.mass,
                                     spec.metallicity, spec.age, spec.velocity,
                                     spec.velocity_axis, perm, offs, nseg, dust_av=spec.dust_av,
                                     dust_exponent=spec.dust_exponent,
                                     lsf_taps=lsf_handoff.taps if fuse else None,
-                                    lsf_crop=EXTEND_FACTOR)
+                                    lsf_crop=EXTEND_FACTOR, out=out)
         else:
             rows = _spectra_tensor(spec, dev)
             cube = ops.segment_sum_rows(rows, perm, offs, nseg)

@@ -53,14 +53,16 @@ class RubixPipeline:
         self.fuse_frame = fuse_frame
 
     def _get_pipeline_functions(self, handoff: Optional[LsfHandoff] = None,
-                                frame: Optional[FrameHandoff] = None) -> list:
+                                frame: Optional[FrameHandoff] = None,
+                                psf_follows: bool = False) -> list:
         c = self.user_config
         lsf = get_convolve_lsf(c, handoff)
         funcs = [
             get_galaxy_rotation(c, frame), get_filter_particles(c, frame),
             get_spaxel_assignment(c, frame), get_calculate_spectra(c), get_reshape_data(c),
             get_scale_spectrum_by_mass(c), get_doppler_shift_and_resampling(c),
-            get_calculate_datacube(c, handoff), get_convolve_psf(c), lsf, get_apply_noise(c),
+            get_calculate_datacube(c, handoff, psf_follows), get_convolve_psf(c), lsf,
+            get_apply_noise(c),
         ]
         # rubix builds calculate_extinction for every pipeline (core/pipeline.py:114);
         # here it is built when the configuration has a dust section
@@ -75,8 +77,12 @@ class RubixPipeline:
         names = step_names(self.pipeline_config)
         lsf = LsfHandoff() if self.fuse_lsf and lsf_fusable(names) else None
         frame = frame_fusion(names) if self.fuse_frame else None
+        # calculate_datacube writes TMA-ready (16-byte) spaxel rows when convolve_psf,
+        # which replaces the cube with a dense one, runs directly after it
+        i = names.index("calculate_datacube") if "calculate_datacube" in names else -1
+        psf_follows = 0 <= i < len(names) - 1 and names[i + 1] == "convolve_psf"
         self._pipeline = LinearTransformerPipeline(
-            self.pipeline_config, self._get_pipeline_functions(lsf, frame))
+            self.pipeline_config, self._get_pipeline_functions(lsf, frame, psf_follows))
         self.func = self._pipeline.expression
         out = self.func(self.data)
         import torch

@@ -6,6 +6,8 @@ from typing import Callable
 
 import numpy as np
 
+import torch
+
 from .. import ops
 from .. import telescope as tel
 from ..logging import get_logger
@@ -43,7 +45,14 @@ def get_convolve_psf(config: dict) -> Callable:
     def convolve_psf(rubixdata: RubixData) -> RubixData:
         """Convolve the input datacube with the PSF kernel."""
         logger.info("Convolving with PSF...")
-        cube = to_device(rubixdata.stars.datacube, dev)
+        cube = rubixdata.stars.datacube
+        # a device cube with unit wavelength stride goes in as it is: the PSF takes any
+        # spaxel stride (calculate_datacube's 16-byte rows included) and writes a dense cube
+        on_dev = (isinstance(cube, torch.Tensor) and cube.is_cuda
+                  and (dev.index is None or cube.device.index == dev.index))
+        if not (on_dev and cube.dim() == 3 and cube.dtype == torch.float32
+                and cube.stride(2) == 1):
+            cube = to_device(cube, dev)
         rubixdata.stars.datacube = ops.psf_forward(cube, taps_y, taps_x)
         return rubixdata
 
