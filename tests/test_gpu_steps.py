@@ -255,3 +255,28 @@ def test_rubix_pipeline_from_galaxy_file(tmp_path):
     want = RubixPipeline(cfg, direct).run().stars.datacube
     torch.cuda.synchronize()
     assert torch.equal(got, want)
+
+
+@pytest.mark.parametrize("n_wave_t", [3721, 256])
+def test_render_pads_the_accumulate_stage_for_the_psf(n_wave_t):
+    """With a PSF the renderer writes the accumulate stage into rows of L rounded up to a
+    multiple of 4 floats (so the PSF stages them by TMA): the stage is a [S, S, L] view
+    with that spaxel stride, and the final cube is dense and bit-identical to the PSF of
+    a dense copy of the stage (the 4-byte-copy kernel).  A multiple of 4 needs no
+    padding."""
+    import torch
+
+    from rubix_gb300.api import IFURenderer
+
+    w = workload("small", n=3000, n_wave_t=n_wave_t)
+    p = w.particles
+    r = IFURenderer.from_workload(w, device="cuda")
+    st = r.render(*(to_dev(a) for a in (p.coords, p.velocity, p.mass, p.metallicity, p.age)))
+    L = w.wave_t.size
+    assert st.cube.shape == (w.sbin, w.sbin, L)
+    assert st.cube.stride(1) == (L + 3) // 4 * 4 and st.cube.stride(2) == 1
+    assert st.final.is_contiguous()
+    dense = st.cube.contiguous()
+    again = r.psf(dense)
+    torch.cuda.synchronize()
+    assert torch.equal(st.final, again)
