@@ -112,7 +112,10 @@ class DatacubeFunction(torch.autograd.Function):
         lsf_t = _lsf_taps(sigma_lsf, wave_res)
         psf_t = _psf_taps(sigma_psf, int(psf_size))
         crop = (len(lsf_t[0]) - 1) // 2
-        Q = ops.lsf_forward(A, lsf_t[0], crop)
+        # Q with 16-byte spaxel rows: the PSF and the sigma_PSF gradient stage them by TMA
+        L = A.shape[-1]
+        Q = torch.empty((nseg, (L + 3) // 4 * 4), dtype=torch.float32, device=A.device)[:, :L]
+        Q = ops.lsf_forward(A, lsf_t[0], crop, out=Q)
         cube = ops.psf_forward(Q.view(r.sbin, r.sbin, -1), psf_t[0])
         ctx.save_for_backward(mass, metallicity, age, velocity, A, Q)
         ctx.r = r

@@ -406,9 +406,15 @@ __host__ __device__ constexpr int psf_tma_stages(int M) {
              : (48 * 1024 - 256) / ((kPsfTileX + M - 1) * kPsfTileL * 4);
 }
 
-template <int M>
+// kDevTaps: the taps come from device memory (a.ty_dev, a.tx_dev; the differentiable
+// render) and the x taps are held in registers too.  kDot: instead of storing an output
+// o[y][x][l], add w[y][x][l] * o into a deterministic sum (w has the output's layout,
+// spaxel stride a.sout; the row's weights are loaded before its x-pass).
+template <int M, bool kDevTaps = false, bool kDot = false>
 __global__ void __launch_bounds__(kPsfThreads, 2)
-    psf_tma_kernel(const __grid_constant__ CUtensorMap map, PsfArgs a) {
+    psf_tma_kernel(const __grid_constant__ CUtensorMap map, PsfArgs a,
+                   const float* __restrict__ w = nullptr, FusedDotScratch* dot_ws = nullptr,
+                   double* dot_out = nullptr) {
   constexpr int W = kPsfTileX + M - 1;  // staged row width
   constexpr int kS = psf_tma_stages(M);
   static_assert(kS >= 3, "PSF ring needs at least 3 rows");
@@ -453,9 +459,14 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
 #pragma unroll
   for (int i = 0; i < M; ++i) {
     unsigned long long v;
-    asm volatile("mov.b64 %0, {%1, %1};" : "=l"(v) : "f"(a.ty[i]));
+    const float t = kDevTaps ? a.ty_dev[i] : a.ty[i];
+    asm volatile("mov.b64 %0, {%1, %1};" : "=l"(v) : "f"(t));
     typ[i] = *reinterpret_cast<const float2*>(&v);
   }
+  float txr[M];  // device x taps in registers (host taps are read from the parameters)
+#pragma unroll
+  for (int i = 0; i < M; ++i) txr[i] = kDevTaps ? a.tx_dev[i] : 0.f;
+  float dot = 0.f;
   for (int r0 = 0; r0 < total; r0 += M) {
 #pragma unroll
     for (int jj = 0; jj < M; ++jj) {
@@ -480,6 +491,16 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
           tensor_copy_3d_g2s(s_in[rn % kS], &map, l0, xsrc0, rn, &s_bar[rn % kS]);
         }
       }
+      // dot mode: this row's output weights, loaded now so the x-pass hides them
+      float wv[kPsfXB];
+      if constexpr (kDot) {
+        const int yw = r - oy;
+#pragma unroll
+        for (int j = 0; j < kPsfXB; ++j) {
+          const int x = x0 + xb + j;
+          wv[j] = (yw >= 0 && l < nl && x < nx) ? w[((long long)yw * nx + x) * sout + l] : 0.f;
+        }
+      }
       // x-pass: scalar FMAs, the taps straight from the kernel parameters
       const float* row = s_in[slot];
       float xv[kPsfXB + M - 1];
@@ -490,7 +511,8 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
       for (int j = 0; j < kPsfXB; ++j) {
         float v = 0.f;
 #pragma unroll
-        for (int i = 0; i < M; ++i) v = fmaf(a.tx[i], xv[j + (M - 1) - i], v);
+        for (int i = 0; i < M; ++i)
+          v = fmaf(kDevTaps ? txr[i] : a.tx[i], xv[j + (M - 1) - i], v);
         hs[j] = v;
       }
       win[jj][0] = make_float2(hs[0], hs[1]);
@@ -504,14 +526,26 @@ __global__ void __launch_bounds__(kPsfThreads, 2)
           o0 = __ffma2_rn(typ[i], win[(jj - i + M) % M][0], o0);
           o1 = __ffma2_rn(typ[i], win[(jj - i + M) % M][1], o1);
         }
-        const int x = x0 + xb;
-        float* o = out + ((long long)y * nx + x) * sout + l;
-        if (x < nx) o[0] = o0.x;
-        if (x + 1 < nx) o[sout] = o0.y;
-        if (x + 2 < nx) o[2 * sout] = o1.x;
-        if (x + 3 < nx) o[3 * sout] = o1.y;
+        if constexpr (kDot) {
+          dot = fmaf(wv[0], o0.x, dot);  // wv = 0 outside the cube
+          dot = fmaf(wv[1], o0.y, dot);
+          dot = fmaf(wv[2], o1.x, dot);
+          dot = fmaf(wv[3], o1.y, dot);
+        } else {
+          const int x = x0 + xb;
+          float* o = out + ((long long)y * nx + x) * sout + l;
+          if (x < nx) o[0] = o0.x;
+          if (x + 1 < nx) o[sout] = o0.y;
+          if (x + 2 < nx) o[2 * sout] = o1.x;
+          if (x + 3 < nx) o[3 * sout] = o1.y;
+        }
       }
     }
+  }
+  if constexpr (kDot) {
+    __shared__ double s_red[kPsfThreads / 32];
+    __shared__ int s_last;
+    fused_dot_finish(dot, dot_ws, dot_out, s_red, &s_last);
   }
 }
 
@@ -535,9 +569,11 @@ EncodeTiledFn encode_tiled() {
 }
 
 // The TMA-staged kernel when the input allows tiled copies (16-byte aligned base, spaxel
-// stride a multiple of 4 floats); false (nothing launched) otherwise.
+// stride a multiple of 4 floats); false (nothing launched) otherwise.  With `w` the dot
+// mode (device taps) into *dot_out.
 template <int M>
-bool launch_psf_tma(const PsfArgs& a, cudaStream_t st) {
+bool launch_psf_tma(const PsfArgs& a, cudaStream_t st, const float* w = nullptr,
+                    FusedDotScratch* dot_ws = nullptr, double* dot_out = nullptr) {
   if (a.sin % 4 != 0 || (reinterpret_cast<uintptr_t>(a.in) & 15) != 0) return false;
   const EncodeTiledFn enc = encode_tiled();
   if (enc == nullptr) return false;
@@ -553,7 +589,12 @@ bool launch_psf_tma(const PsfArgs& a, cudaStream_t st) {
           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
   dim3 grid(div_up(a.nx, kPsfTileX), div_up(a.nl, kPsfTileL));
-  psf_tma_kernel<M><<<grid, kPsfThreads, 0, st>>>(map, a);
+  if (w != nullptr)
+    psf_tma_kernel<M, true, true><<<grid, kPsfThreads, 0, st>>>(map, a, w, dot_ws, dot_out);
+  else if (a.ty_dev != nullptr)
+    psf_tma_kernel<M, true><<<grid, kPsfThreads, 0, st>>>(map, a);
+  else
+    psf_tma_kernel<M><<<grid, kPsfThreads, 0, st>>>(map, a);
   return true;
 }
 
@@ -593,13 +634,14 @@ __global__ void __launch_bounds__(kPsfThreads) ragged_psf_kernel(RaggedPsfArgs a
 template <int M>
 int launch_psf_reg(const PsfArgs& a, cudaStream_t st) {
   dim3 grid(div_up(a.nx, kPsfTileX), div_up(a.nl, kPsfTileL));
-  // host taps: the packed-FMA kernel with the taps as parameters (up to 17 taps, where
-  // its window stays in registers), its rows staged by TMA where the stride allows
+  // rows staged by TMA where the stride allows (up to 17 taps, where the window and the
+  // tap pairs stay in registers), host or device taps
+  if (M <= 17 && launch_psf_tma<(M <= 17 ? M : 17)>(a, st)) {
+    RUBIX_LAUNCH_CHECK("psf_tma_kernel");
+    return RUBIX_OK;
+  }
+  // host taps: the packed-FMA kernel with the taps as parameters
   if (a.ty_dev == nullptr && M <= 17) {
-    if (launch_psf_tma<(M <= 17 ? M : 17)>(a, st)) {
-      RUBIX_LAUNCH_CHECK("psf_tma_kernel");
-      return RUBIX_OK;
-    }
     psf_reg2_kernel<(M <= 17 ? M : 17)><<<grid, kPsfThreads, 0, st>>>(a);
     RUBIX_LAUNCH_CHECK("psf_reg2_kernel");
     return RUBIX_OK;
@@ -744,6 +786,28 @@ extern "C" int rubix_psf_dot_dtaps(const float* in, int64_t spaxel_stride_in, co
   a.tx_dev = tx;
   auto* scratch = static_cast<FusedDotScratch*>(workspace);
   RUBIX_CUDA_TRY(cudaMemsetAsync(&scratch->counter, 0, sizeof(unsigned), st));
+  // rows staged by TMA where the input's stride allows (m <= 17), else 4-byte copies
+  bool tma = false;
+  switch (m) {
+#define RUBIX_PSF_DOT_TMA(MM) \
+  case MM: tma = launch_psf_tma<MM>(a, st, w, scratch, out); break;
+    RUBIX_PSF_DOT_TMA(1)
+    RUBIX_PSF_DOT_TMA(3)
+    RUBIX_PSF_DOT_TMA(5)
+    RUBIX_PSF_DOT_TMA(7)
+    RUBIX_PSF_DOT_TMA(9)
+    RUBIX_PSF_DOT_TMA(11)
+    RUBIX_PSF_DOT_TMA(13)
+    RUBIX_PSF_DOT_TMA(15)
+    RUBIX_PSF_DOT_TMA(17)
+#undef RUBIX_PSF_DOT_TMA
+    default:
+      break;
+  }
+  if (tma) {
+    RUBIX_LAUNCH_CHECK("psf_tma_kernel");
+    return RUBIX_OK;
+  }
   switch (m) {
 #define RUBIX_PSF_DOT(MM)                                                   \
   case MM:                                                                  \
