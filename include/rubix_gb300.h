@@ -301,7 +301,8 @@ RUBIX_API int rubix_fits_cube_layout(const float* cube, int32_t A, int32_t B, in
 /*
  * rubix_psf_fwd and rubix_lsf_fwd with the taps in device memory (ty, tx, taps are
  * device pointers of m_y, m_x, n_taps floats), so that taps computed on the device
- * (rubix_gauss_taps) need no copy to the host.  Same arguments, limits and results.
+ * (rubix_gauss_taps) need no copy to the host.  Same arguments, limits and results
+ * (including the TMA staging of 16-byte spaxel rows and rubix_psf_status).
  */
 RUBIX_API int rubix_psf_fwd_dtaps(const float* in, float* out, int32_t ny, int32_t nx,
                                   int32_t n_wave_t, int64_t spaxel_stride_in,
