@@ -160,10 +160,15 @@ def test_fits_layout_kernel_matches_numpy(tmp_path):
     from rubix_gb300.core.fits import cube_fits_bytes, store_fits
 
     rng = np.random.default_rng(2)
-    for shape in ((25, 25, 3721), (33, 7, 45), (1, 1, 1), (70, 40, 33)):
+    for shape in ((25, 25, 3721), (33, 7, 45), (1, 1, 1), (70, 40, 33), (65, 3, 129)):
         cube = rng.standard_normal(shape).astype(np.float32)
         got = cube_fits_bytes(torch.from_numpy(cube).cuda())
         assert got == cube_fits_bytes(cube), shape
+    # a cube with a padded spaxel stride (the renderer's accumulate stage)
+    cube = rng.standard_normal((20, 21, 47)).astype(np.float32)
+    padded = torch.zeros((20, 21, 48), device="cuda")
+    padded[:, :, :47] = torch.from_numpy(cube).cuda()
+    assert cube_fits_bytes(padded[:, :, :47]) == cube_fits_bytes(cube)
     cube = rng.standard_normal((30, 30, 300)).astype(np.float32)
     d = RubixData()
     d.stars.datacube = torch.from_numpy(cube).cuda()
