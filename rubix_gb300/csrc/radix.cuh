@@ -1,7 +1,9 @@
 // Stable LSD radix sort of (32-bit key, int value) pairs, 8 bits per pass, written
 // from the published LSD scheme: per pass, a per-tile digit histogram, one exclusive
 // scan over (digit, tile), and a stable scatter in which each tile ranks its keys with
-// warp-level match/popc and per-warp digit counters.  Deterministic.
+// warp-level match/popc and per-warp digit counters, reorders them by digit in shared
+// memory and writes each digit's run with consecutive threads on consecutive addresses
+// (coalesced stores instead of one scattered store per key).  Deterministic.
 #pragma once
 
 #include "common.cuh"
@@ -80,6 +82,9 @@ radix_scatter_kernel(const unsigned* __restrict__ keys_in, const int* __restrict
   __shared__ int s_cnt[kWarps][kRadix];
   __shared__ int s_base[kRadix];
   __shared__ int s_dw[kWarps];
+  __shared__ int s_tstart[kRadix];  // start of digit d in the tile's digit-ordered copy
+  __shared__ unsigned s_k[kSortTile];
+  __shared__ int s_v[kSortTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kWarps * kRadix; i += kSortThreads) (&s_cnt[0][0])[i] = 0;
   const int n_digits = (int)digit_mask + 1;
@@ -124,26 +129,54 @@ radix_scatter_kernel(const unsigned* __restrict__ keys_in, const int* __restrict
     __syncwarp();
   }
   __syncthreads();
-  // Exclusive prefix over warps, per digit.
-  for (int d = threadIdx.x; d < n_digits; d += kSortThreads) {
+  // Exclusive prefix over warps, per digit (one digit per thread), and the tile's count
+  // of each digit, scanned over the digits into the digit's start in the tile.
+  {
+    const int d = threadIdx.x;
     int run = 0;
+    if (d < n_digits) {
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      int c = s_cnt[w][d];
-      s_cnt[w][d] = run;
-      run += c;
+      for (int w = 0; w < kWarps; ++w) {
+        int c = s_cnt[w][d];
+        s_cnt[w][d] = run;
+        run += c;
+      }
     }
+    int x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_dw[warp] = x;
+    __syncthreads();
+    int before = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) before += w < warp ? s_dw[w] : 0;
+    s_tstart[d] = before + x - run;
   }
   __syncthreads();
+  // the tile in (digit, original position) order in shared memory
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     long long e = wbase + r * 32 + lane;
     if (e < n) {
       int d = (int)((key[r] >> shift) & digit_mask);
-      long long pos = (long long)s_base[d] + s_cnt[warp][d] + rank[r];
-      keys_out[pos] = key[r];
-      vals_out[pos] = val[r];
+      const int lpos = s_tstart[d] + s_cnt[warp][d] + rank[r];
+      s_k[lpos] = key[r];
+      s_v[lpos] = val[r];
     }
+  }
+  __syncthreads();
+  // each digit's run to its place: consecutive threads, consecutive addresses
+  const long long tile0 = (long long)blockIdx.x * kSortTile;
+  const int tile_n = (int)min((long long)kSortTile, n - tile0);
+  for (int i = threadIdx.x; i < tile_n; i += kSortThreads) {
+    const unsigned k = s_k[i];
+    const int d = (int)((k >> shift) & digit_mask);
+    const long long pos = (long long)s_base[d] + (i - s_tstart[d]);
+    keys_out[pos] = k;
+    vals_out[pos] = s_v[i];
   }
 }
 
